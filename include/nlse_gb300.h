@@ -1,0 +1,162 @@
+/*
+ * libnlse_sm103 — C ABI of the GB300 (sm_103a) split-step Fourier engine.
+ *
+ * The library replaces the device work of the reference package's GPU
+ * backend (Quantum-Optics-LKB/NLSE v2.3.0, backend="GPU"): VkFFT plans, the
+ * CuPy fused elementwise kernels and the z-loop of out_field.  Every pointer
+ * passed in is a device pointer owned by the caller (Python passes
+ * torch.Tensor.data_ptr()); the plan owns only its own tables.  All calls are
+ * asynchronous on the given stream (a cudaStream_t passed as void*; NULL is
+ * the legacy default stream).  Kernel faults surface at the caller's next
+ * synchronisation.
+ *
+ * Return value of every int function: NLSE_OK (0) or a negative nlse_status;
+ * nlse_last_error() then describes the failure (thread-local string).
+ *
+ * Layout of a field A (C order, complex64 or complex128 interleaved):
+ *   ndim = 1: [nfields][comps][NX]
+ *   ndim = 2: [nfields][comps][NY][NX]
+ *   ndim = 3: [nfields][NY][NX][NT]            (comps = 1)
+ * The transform runs over the ndim trailing axes, batched over the rest, the
+ * way the reference plans VkFFTApp(A.shape, ndim=len(_last_axes)) over the
+ * trailing axes (NLSE/nlse.py:199-218).  Axis lengths are powers of two from
+ * 2 to 4096.
+ */
+#ifndef NLSE_GB300_H
+#define NLSE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NLSE_ABI_VERSION 1
+
+typedef enum { NLSE_C64 = 0, NLSE_C128 = 1 } nlse_dtype;
+
+typedef enum {
+  NLSE_OK = 0,
+  NLSE_ERR_ARG = -1,         /* bad argument (null pointer, bad size, bad flag) */
+  NLSE_ERR_UNSUPPORTED = -2, /* shape or option this build does not implement */
+  NLSE_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+  NLSE_ERR_STATE = -4        /* call not valid in the current state */
+} nlse_status;
+
+/* nlse_propagate flags */
+#define NLSE_RUN_GRAPH 1 /* capture the whole step sequence in a CUDA graph, replay it when
+                            called again with the same pointers and step range */
+
+typedef struct nlse_plan_s* nlse_plan;
+
+/* Geometry of the fields a plan transforms. */
+typedef struct {
+  int32_t ndim;     /* 1, 2 or 3 transform axes */
+  int64_t shape[3]; /* transform lengths, outermost first: {NX}, {NY,NX}, {NY,NX,NT} */
+  int64_t nfields;  /* independent fields (product of the leading dimensions) */
+  int32_t comps;    /* components per field: 1, or 2 (CNLSE/DDGPE, stacked before the axes) */
+  int32_t dtype;    /* nlse_dtype of the field */
+} nlse_desc;
+
+/*
+ * Per-field parameter block: nfields x NLSE_PARAM_STRIDE doubles in device
+ * memory.  Index [set*16 + comp*7 + k], set 0 = the nonlinear step after the
+ * linear step, set 1 = the half step before it ("double" scheme), k:
+ *   0 dz, 1 alpha (already halved as the reference passes alpha/2),
+ *   2 g_self, 3 g_cross, 4 Isat_self, 5 Isat_cross (converted units, inf for
+ *   none), 6 vscale (V' = vscale * V).
+ * [14], [15]: cos and sin of (omega/2)*dz for the Rabi rotation.
+ * [30]: dz of the DDGPE pump term.
+ */
+#define NLSE_PARAM_STRIDE 32
+
+/* The operator of one split step. */
+typedef struct {
+  const void* V;         /* potential, or NULL */
+  int32_t v_complex;     /* V holds complex values (else real) */
+  int32_t v_f32;         /* V stored in single precision (else double) */
+  int64_t v_fstride;     /* elements between two fields' potentials; 0 = shared */
+  const void* prop;      /* linear propagator, [comps][transform axes] */
+  int32_t prop_c128;     /* propagator stored as complex128 (else complex64) */
+  int64_t prop_cstride;  /* elements between the components' propagators; 0 = shared */
+  const double* params;  /* per-field parameter block, see above */
+  int32_t scheme;        /* 0 = "single" (Lie), 1 = "double" (Strang) */
+  int32_t rabi;          /* apply the Rabi rotation after the nonlinear step */
+  const void* pump_r;    /* DDGPE pump spatial profile [pixels] (field dtype) or NULL */
+  const void* pump_t;    /* DDGPE pump time profile [steps] (field dtype) */
+  const void* probe_r;   /* DDGPE probe spatial profile or NULL */
+  const void* probe_t;
+} nlse_operator;
+
+/* ABI version of the loaded library (NLSE_ABI_VERSION). */
+int nlse_abi_version(void);
+
+/* Description of the last error on this thread ("" if none). */
+const char* nlse_last_error(void);
+
+/*
+ * Create a plan on the current CUDA device: validates the geometry, uploads
+ * the twiddle table and sets the kernel attributes.  Replaces
+ * NLSE._build_fft_plan (NLSE/nlse.py:199-218).
+ */
+int nlse_plan_create(nlse_plan* out, const nlse_desc* desc);
+int nlse_plan_destroy(nlse_plan plan);
+
+/*
+ * Advance A in place by nsteps split steps of the reference's
+ * NLSE.split_step (NLSE/nlse.py:372-487), CNLSE.split_step
+ * (NLSE/cnlse.py:204-423) or DDGPE.split_step (NLSE/ddgpe.py:247-457), i.e.
+ * the body of the out_field z-loop (NLSE/nlse.py:570-588) without callbacks.
+ * step0 is the loop index of the first step (selects pump_t[step0 + s]).
+ * A is in real space on entry and on return.
+ */
+int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nsteps,
+                   int64_t step0, int32_t flags, void* stream);
+
+/*
+ * In-place transform over the plan's axes: forward (inverse = 0) or
+ * normalised inverse (inverse = 1), matching VkFFTApp.fft / .ifft with
+ * norm=1 (NLSE/nlse.py:435,438).
+ */
+int nlse_fft(nlse_plan plan, void* A, int32_t inverse, void* stream);
+
+/*
+ * Only the nonlinear step (parameter set 0, optional Rabi and pump) applied
+ * pointwise to A: kernels_gpu.nl_prop / nl_prop_without_V / nl_prop_c /
+ * nl_prop_without_V_c / rabi_coupling (NLSE/kernels_gpu.py:4-156) and
+ * DDGPE.laser_excitation (NLSE/ddgpe.py:127-156).  asq: optional
+ * [nfields][comps][pixels] real array used as |A|^2 (the reference's A_sq
+ * after its nonlocal convolution); NULL computes |A|^2 from A.
+ */
+int nlse_nonlinear(nlse_plan plan, void* A, const void* asq, const nlse_operator* op,
+                   int64_t step, void* stream);
+
+/*
+ * Per-segment sum of |A|^2 accumulated in FP64 (the integral of
+ * _prepare_output_array, NLSE/nlse.py:293-303, and the callbacks' norms,
+ * NLSE/callbacks.py:32-54).  A has nseg segments of seg_len elements; out
+ * receives nseg doubles.  workspace: device scratch of at least
+ * nlse_power_workspace_size(nseg, seg_len) bytes.
+ */
+size_t nlse_power_workspace_size(int64_t nseg, int64_t seg_len);
+int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, double* out,
+               void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Power normalisation of _prepare_output_array (NLSE/nlse.py:284-307):
+ * out[s] = in[s] * sqrt(target[s] / (sums[s] * coef)), the factor rounded to
+ * the field precision.  in may equal out.
+ */
+int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64_t seg_len,
+                   const double* sums, const double* target, double coef, void* stream);
+
+/* |A|^2 into a real array of the field precision (kernels_gpu.square_mod,
+ * NLSE/kernels_gpu.py:179-190). */
+int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLSE_GB300_H */

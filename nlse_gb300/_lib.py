@@ -1,0 +1,130 @@
+"""ctypes binding of libnlse_sm103 (include/nlse_gb300.h).
+
+The library is built in-tree by ``nlse_gb300._build.build()``.  Loading fails
+loudly when it is missing: there is no fallback implementation.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import threading
+from pathlib import Path
+
+from . import _build
+
+NLSE_C64 = 0
+NLSE_C128 = 1
+NLSE_RUN_GRAPH = 1
+NLSE_PARAM_STRIDE = 32
+
+OK = 0
+ERR_ARG = -1
+ERR_UNSUPPORTED = -2
+ERR_CUDA = -3
+ERR_STATE = -4
+
+
+class Desc(ct.Structure):
+    _fields_ = [
+        ("ndim", ct.c_int32),
+        ("shape", ct.c_int64 * 3),
+        ("nfields", ct.c_int64),
+        ("comps", ct.c_int32),
+        ("dtype", ct.c_int32),
+    ]
+
+
+class Operator(ct.Structure):
+    _fields_ = [
+        ("V", ct.c_void_p),
+        ("v_complex", ct.c_int32),
+        ("v_f32", ct.c_int32),
+        ("v_fstride", ct.c_int64),
+        ("prop", ct.c_void_p),
+        ("prop_c128", ct.c_int32),
+        ("prop_cstride", ct.c_int64),
+        ("params", ct.c_void_p),
+        ("scheme", ct.c_int32),
+        ("rabi", ct.c_int32),
+        ("pump_r", ct.c_void_p),
+        ("pump_t", ct.c_void_p),
+        ("probe_r", ct.c_void_p),
+        ("probe_t", ct.c_void_p),
+    ]
+
+
+# (name, restype, argtypes) for every symbol declared in include/nlse_gb300.h
+SIGNATURES = [
+    ("nlse_abi_version", ct.c_int, []),
+    ("nlse_last_error", ct.c_char_p, []),
+    ("nlse_plan_create", ct.c_int, [ct.POINTER(ct.c_void_p), ct.POINTER(Desc)]),
+    ("nlse_plan_destroy", ct.c_int, [ct.c_void_p]),
+    (
+        "nlse_propagate",
+        ct.c_int,
+        [ct.c_void_p, ct.c_void_p, ct.POINTER(Operator), ct.c_int64, ct.c_int64, ct.c_int32,
+         ct.c_void_p],
+    ),
+    ("nlse_fft", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
+    (
+        "nlse_nonlinear",
+        ct.c_int,
+        [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(Operator), ct.c_int64, ct.c_void_p],
+    ),
+    ("nlse_power_workspace_size", ct.c_size_t, [ct.c_int64, ct.c_int64]),
+    (
+        "nlse_power",
+        ct.c_int,
+        [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_size_t,
+         ct.c_void_p],
+    ),
+    (
+        "nlse_normalize",
+        ct.c_int,
+        [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p,
+         ct.c_double, ct.c_void_p],
+    ),
+    ("nlse_square_mod", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_void_p]),
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str | Path | None = None) -> ct.CDLL:
+    """Load (once) and return the library, with prototypes set."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = Path(path) if path else _build.lib_path()
+        if not p.exists():
+            raise RuntimeError(
+                f"{p} is missing: build it with nlse_gb300._build.build() "
+                "(nvcc, sm_103a); the engine has no CPU fallback"
+            )
+        lib = ct.CDLL(str(p))
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.nlse_abi_version() != 1:
+            raise RuntimeError("libnlse_sm103 ABI version mismatch")
+        _lib = lib
+        return lib
+
+
+def last_error() -> str:
+    return load().nlse_last_error().decode(errors="replace")
+
+
+def check(rc: int, what: str = "") -> None:
+    """Raise the Python exception matching a negative status."""
+    if rc == OK:
+        return
+    msg = f"{what}: {last_error()}" if what else last_error()
+    if rc == ERR_ARG:
+        raise ValueError(msg)
+    if rc == ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise RuntimeError(msg)

@@ -1,0 +1,468 @@
+// C ABI of libnlse_sm103: plans, the split-step sequence and CUDA-graph
+// replay of the z-loop.  Declarations and contracts: include/nlse_gb300.h.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "launch.h"
+#include "nlse_gb300.h"
+
+using namespace nlse;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(NLSE_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define NLSE_CUDA(call, what)                  \
+  do {                                         \
+    cudaError_t e_ = (call);                   \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// Twiddle tables w[m] = exp(-2*pi*i*m/kNMax), one per device and precision,
+// computed in long double and rounded once.
+constexpr int kMaxDevices = 64;
+std::mutex g_tw_mu;
+void* g_tw[kMaxDevices][2] = {};
+
+int get_twiddles(int dev, int dtype, const void** out) {
+  if (dev < 0 || dev >= kMaxDevices) return fail(NLSE_ERR_UNSUPPORTED, "device ordinal %d", dev);
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  if (!g_tw[dev][dtype]) {
+    const long double pi = 3.141592653589793238462643383279502884L;
+    std::vector<double> hd(2 * (size_t)kNMax);
+    for (int m = 0; m < kNMax; ++m) {
+      const long double ang = 2.0L * pi * (long double)m / (long double)kNMax;
+      hd[2 * m] = (double)cosl(ang);
+      hd[2 * m + 1] = (double)(-sinl(ang));
+    }
+    void* d = nullptr;
+    size_t bytes;
+    if (dtype == NLSE_C64) {
+      std::vector<float> hf(2 * (size_t)kNMax);
+      for (size_t i = 0; i < hf.size(); ++i) hf[i] = (float)hd[i];
+      bytes = hf.size() * sizeof(float);
+      NLSE_CUDA(cudaMalloc(&d, bytes), "cudaMalloc(twiddles)");
+      NLSE_CUDA(cudaMemcpy(d, hf.data(), bytes, cudaMemcpyHostToDevice), "cudaMemcpy(twiddles)");
+    } else {
+      bytes = hd.size() * sizeof(double);
+      NLSE_CUDA(cudaMalloc(&d, bytes), "cudaMalloc(twiddles)");
+      NLSE_CUDA(cudaMemcpy(d, hd.data(), bytes, cudaMemcpyHostToDevice), "cudaMemcpy(twiddles)");
+    }
+    g_tw[dev][dtype] = d;
+  }
+  *out = g_tw[dev][dtype];
+  return NLSE_OK;
+}
+
+int ilog2_pow2(int64_t n) {
+  if (n < 2 || (n & (n - 1))) return -1;
+  int l = 0;
+  while ((int64_t(1) << l) < n) ++l;
+  return l;
+}
+
+struct GraphKey {
+  void* A;
+  nlse_operator op;
+  int64_t nsteps, step0;
+  bool operator==(const GraphKey& o) const {
+    return A == o.A && nsteps == o.nsteps && step0 == o.step0 &&
+           std::memcmp(&op, &o.op, sizeof(op)) == 0;
+  }
+};
+
+}  // namespace
+
+struct nlse_plan_s {
+  nlse_desc d;
+  int dev = 0;
+  const void* tw = nullptr;
+  int lg[3] = {0, 0, 0};
+  int64_t pix = 0;  // pixels of one component of one field
+  cudaStream_t cap = nullptr;  // private stream used only for graph capture
+  cudaGraphExec_t gexec = nullptr;
+  GraphKey gkey;
+  bool gvalid = false;
+};
+
+namespace {
+
+cudaError_t rows(const nlse_plan_s* p, int mode, int log2n, const StepArgs& a, cudaStream_t s,
+                 bool prep = false) {
+  if (p->d.dtype == NLSE_C64)
+    return a.comps == 1 ? launch_rows_f32_c1(mode, log2n, a, s, prep)
+                        : launch_rows_f32_c2(mode, log2n, a, s, prep);
+  return a.comps == 1 ? launch_rows_f64_c1(mode, log2n, a, s, prep)
+                      : launch_rows_f64_c2(mode, log2n, a, s, prep);
+}
+
+cudaError_t cols(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a, cudaStream_t s,
+                 bool prep = false) {
+  if (p->d.dtype == NLSE_C64) return launch_cols_f32(mode, log2n, a, s, prep);
+  return launch_cols_f64(mode, log2n, a, s, prep);
+}
+
+// Columns per column-pass CTA: 64-byte row segments, bounded by the thread
+// budget of one CTA and by the contiguous extent available.
+int pick_w(const nlse_plan_s* p, int log2n, int64_t inner) {
+  const int tpl = (1 << log2n) >= 16 ? (1 << log2n) / 16 : 1;
+  int w = p->d.dtype == NLSE_C64 ? 8 : 4;
+  while (w > 1 && (w * tpl > kColMaxThreads || w > inner || inner % w)) w >>= 1;
+  return w;
+}
+
+// Column-pass arguments for axis `axis` (0 = outermost transform axis) of an
+// ndim-D field.
+ColArgs col_args(const nlse_plan_s* p, void* A, const nlse_operator* op, int axis) {
+  const nlse_desc& d = p->d;
+  ColArgs c{};
+  c.A = A;
+  c.tw = p->tw;
+  c.prop = op ? op->prop : nullptr;
+  c.prop_cstride = op ? op->prop_cstride : 0;
+  c.flags = (op && op->prop_c128) ? F_PROP_C128 : 0u;
+  c.comps = d.comps;
+  int64_t inner = 1;
+  for (int k = axis + 1; k < d.ndim; ++k) inner *= d.shape[k];
+  const int64_t n = d.shape[axis];
+  int64_t outer = d.nfields * d.comps;
+  for (int k = 0; k < axis; ++k) outer *= d.shape[k];
+  c.w = pick_w(p, p->lg[axis], inner);
+  c.ld = inner;
+  c.outer_stride = n * inner;
+  c.ncb = inner / c.w;
+  c.nblocks = c.ncb * outer;
+  return c;
+}
+
+StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
+  const nlse_desc& d = p->d;
+  StepArgs a{};
+  a.A = A;
+  a.tw = p->tw;
+  const int64_t n = d.shape[d.ndim - 1];
+  a.lines_per_comp = p->pix / n;
+  a.nq = d.nfields * a.lines_per_comp;
+  a.pix = p->pix;
+  a.inv_n = 1.0 / (double)p->pix;
+  a.comps = d.comps;
+  a.nsteps = 1;
+  if (op) {
+    a.V = op->V;
+    a.prop = op->prop;
+    a.params = op->params;
+    a.pump_r = op->pump_r;
+    a.pump_t = op->pump_t;
+    a.probe_r = op->probe_r;
+    a.probe_t = op->probe_t;
+    a.v_fstride = op->v_fstride;
+    a.prop_cstride = op->prop_cstride;
+    uint32_t f = 0;
+    if (op->V) f |= F_HAS_V;
+    if (op->v_complex) f |= F_V_COMPLEX;
+    if (op->v_f32) f |= F_V_F32;
+    if (op->prop_c128) f |= F_PROP_C128;
+    if (op->rabi && d.comps == 2 && op->scheme == 0) f |= F_RABI;
+    if (op->pump_r && d.comps == 2) f |= F_PUMP;
+    if (op->probe_r && d.comps == 2) f |= F_PROBE;
+    a.flags = f;
+  }
+  return a;
+}
+
+int check_op(const nlse_plan_s* p, const nlse_operator* op) {
+  if (!op) return fail(NLSE_ERR_ARG, "operator is NULL");
+  if (!op->prop) return fail(NLSE_ERR_ARG, "propagator is NULL");
+  if (!op->params) return fail(NLSE_ERR_ARG, "parameter block is NULL");
+  if (op->scheme != 0 && op->scheme != 1) return fail(NLSE_ERR_ARG, "scheme must be 0 or 1");
+  if (p->d.dtype == NLSE_C64 && op->V && !op->v_f32)
+    return fail(NLSE_ERR_ARG, "a complex64 field needs a single-precision potential");
+  if ((op->pump_r && !op->pump_t) || (op->probe_r && !op->probe_t))
+    return fail(NLSE_ERR_ARG, "pump/probe spatial profile given without time profile");
+  if ((op->pump_r || op->probe_r) && (p->d.comps != 2 || p->d.ndim != 2))
+    return fail(NLSE_ERR_UNSUPPORTED, "pump/probe terms need a two-component 2-D field");
+  return NLSE_OK;
+}
+
+// Enqueue nsteps split steps (no capture handling here).
+int enqueue_steps(nlse_plan_s* p, void* A, const nlse_operator* op, int64_t nsteps, int64_t step0,
+                  cudaStream_t s) {
+  const nlse_desc& d = p->d;
+  if (nsteps <= 0) return NLSE_OK;
+  StepArgs a = row_args(p, A, op);
+  const uint32_t pre = op->scheme == 1 ? F_PRE_NL : 0u;
+  const int rl = p->lg[d.ndim - 1];
+  cudaError_t e;
+  if (d.ndim == 1) {
+    a.flags |= pre;
+    if (a.flags & (F_PUMP | F_PROBE)) return fail(NLSE_ERR_UNSUPPORTED, "pump in 1-D");
+    a.nsteps = (int)nsteps;
+    a.step = (int)step0;
+    e = rows(p, ROW_FULL, rl, a, s);
+    if (e != cudaSuccess) return cuda_fail(e, "row pass (1-D full step)");
+    return NLSE_OK;
+  }
+  // first forward row pass, with the step's leading half nonlinear step
+  StepArgs a0 = a;
+  a0.flags |= pre;
+  e = rows(p, ROW_FWD, rl, a0, s);
+  if (e != cudaSuccess) return cuda_fail(e, "row pass (forward)");
+  for (int64_t st = 0; st < nsteps; ++st) {
+    if (d.ndim == 2) {
+      const ColArgs c = col_args(p, A, op, 0);
+      e = cols(p, COL_FWD_PROP_INV, p->lg[0], c, s);
+      if (e != cudaSuccess) return cuda_fail(e, "column pass (linear step)");
+    } else {
+      const ColArgs cx = col_args(p, A, op, 1);
+      const ColArgs cy = col_args(p, A, op, 0);
+      e = cols(p, COL_FWD, p->lg[1], cx, s);
+      if (e == cudaSuccess) e = cols(p, COL_FWD_PROP_INV, p->lg[0], cy, s);
+      if (e == cudaSuccess) e = cols(p, COL_INV, p->lg[1], cx, s);
+      if (e != cudaSuccess) return cuda_fail(e, "column pass (3-D linear step)");
+    }
+    StepArgs ai = a;
+    ai.step = (int)(step0 + st);
+    if (st + 1 < nsteps) {
+      ai.flags |= pre;
+      e = rows(p, ROW_INV_NL_FWD, rl, ai, s);
+    } else {
+      e = rows(p, ROW_INV_NL, rl, ai, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "row pass (inverse + nonlinear)");
+  }
+  return NLSE_OK;
+}
+
+// Raise the dynamic shared-memory limit of every kernel the plan can launch
+// (outside any stream capture).
+int prepare_kernels(nlse_plan_s* p) {
+  StepArgs a = row_args(p, nullptr, nullptr);
+  for (int nc = 1; nc <= p->d.comps; ++nc) {
+    a.comps = nc;
+    for (int m : {ROW_FWD, ROW_INV_NL, ROW_INV_NL_FWD, ROW_FULL, ROW_INV}) {
+      if (m == ROW_INV && nc == 2) continue;
+      cudaError_t e = rows(p, m, p->lg[p->d.ndim - 1], a, nullptr, true);
+      if (e != cudaSuccess) return cuda_fail(e, "kernel attributes (rows)");
+    }
+  }
+  for (int ax = 0; ax + 1 < p->d.ndim; ++ax) {
+    ColArgs c{};
+    for (int m : {COL_FWD, COL_INV, COL_FWD_PROP_INV}) {
+      cudaError_t e = cols(p, m, p->lg[ax], c, nullptr, true);
+      if (e != cudaSuccess) return cuda_fail(e, "kernel attributes (columns)");
+    }
+  }
+  return NLSE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nlse_abi_version(void) { return NLSE_ABI_VERSION; }
+
+const char* nlse_last_error(void) { return g_err.c_str(); }
+
+int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
+  g_err.clear();
+  if (!out || !desc) return fail(NLSE_ERR_ARG, "null argument");
+  *out = nullptr;
+  const nlse_desc& d = *desc;
+  if (d.ndim < 1 || d.ndim > 3) return fail(NLSE_ERR_ARG, "ndim must be 1, 2 or 3 (got %d)", d.ndim);
+  if (d.dtype != NLSE_C64 && d.dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", d.dtype);
+  if (d.comps != 1 && d.comps != 2) return fail(NLSE_ERR_ARG, "comps must be 1 or 2");
+  if (d.ndim == 3 && d.comps != 1)
+    return fail(NLSE_ERR_UNSUPPORTED, "3-D fields have one component");
+  if (d.nfields < 1) return fail(NLSE_ERR_ARG, "nfields must be >= 1");
+  auto* p = new nlse_plan_s();
+  p->d = d;
+  p->pix = 1;
+  for (int k = 0; k < d.ndim; ++k) {
+    const int l = ilog2_pow2(d.shape[k]);
+    if (l < kMinLog2 || l > kMaxLog2) {
+      delete p;
+      return fail(NLSE_ERR_UNSUPPORTED,
+                  "axis %d has length %lld; this build transforms powers of two from 2 to %d", k,
+                  (long long)d.shape[k], 1 << kMaxLog2);
+    }
+    p->lg[k] = l;
+    p->pix *= d.shape[k];
+  }
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  int rc = get_twiddles(p->dev, d.dtype, &p->tw);
+  if (rc == NLSE_OK) rc = prepare_kernels(p);
+  if (rc == NLSE_OK) {
+    e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
+  }
+  if (rc != NLSE_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return NLSE_OK;
+}
+
+int nlse_plan_destroy(nlse_plan p) {
+  if (!p) return NLSE_OK;
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->cap) cudaStreamDestroy(p->cap);
+  delete p;
+  return NLSE_OK;
+}
+
+int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps, int64_t step0,
+                   int32_t flags, void* stream) {
+  g_err.clear();
+  if (!p || !A) return fail(NLSE_ERR_ARG, "null plan or field");
+  if (nsteps < 0 || step0 < 0) return fail(NLSE_ERR_ARG, "negative step count or index");
+  int rc = check_op(p, op);
+  if (rc != NLSE_OK) return rc;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (!(flags & NLSE_RUN_GRAPH)) return enqueue_steps(p, A, op, nsteps, step0, s);
+
+  GraphKey key{A, *op, nsteps, step0};
+  if (!(p->gvalid && p->gkey == key)) {
+    // Capture on the plan's private stream, ordered after the caller's work
+    // only at launch time (the graph itself has no external dependencies).
+    cudaGraph_t g = nullptr;
+    NLSE_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    rc = enqueue_steps(p, A, op, nsteps, step0, p->cap);
+    cudaError_t e = cudaStreamEndCapture(p->cap, &g);
+    if (rc != NLSE_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    bool updated = false;
+    if (p->gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(p->gexec, g, &info) == cudaSuccess) updated = true;
+      else {
+        cudaGetLastError();
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+      }
+    }
+    if (!updated) {
+      e = cudaGraphInstantiate(&p->gexec, g, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        p->gvalid = false;
+        return cuda_fail(e, "graph instantiate");
+      }
+    }
+    cudaGraphDestroy(g);
+    p->gkey = key;
+    p->gvalid = true;
+  }
+  NLSE_CUDA(cudaGraphLaunch(p->gexec, s), "graph launch");
+  return NLSE_OK;
+}
+
+int nlse_fft(nlse_plan p, void* A, int32_t inverse, void* stream) {
+  g_err.clear();
+  if (!p || !A) return fail(NLSE_ERR_ARG, "null plan or field");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const nlse_desc& d = p->d;
+  // components are independent transforms here: view them as fields
+  nlse_plan_s q = *p;
+  q.d.nfields = d.nfields * d.comps;
+  q.d.comps = 1;
+  StepArgs a = row_args(&q, A, nullptr);
+  a.flags = F_NO_POST;
+  const int rl = p->lg[d.ndim - 1];
+  cudaError_t e = cudaSuccess;
+  if (!inverse) {
+    e = rows(&q, ROW_FWD, rl, a, s);
+    for (int ax = d.ndim - 2; ax >= 0 && e == cudaSuccess; --ax)
+      e = cols(&q, COL_FWD, p->lg[ax], col_args(&q, A, nullptr, ax), s);
+  } else {
+    for (int ax = 0; ax + 1 < d.ndim && e == cudaSuccess; ++ax)
+      e = cols(&q, COL_INV, p->lg[ax], col_args(&q, A, nullptr, ax), s);
+    if (e == cudaSuccess) e = rows(&q, ROW_INV, rl, a, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "fft");
+  return NLSE_OK;
+}
+
+int nlse_nonlinear(nlse_plan p, void* A, const void* asq, const nlse_operator* op, int64_t step,
+                   void* stream) {
+  g_err.clear();
+  if (!p || !A || !op || !op->params) return fail(NLSE_ERR_ARG, "null argument");
+  if (p->d.dtype == NLSE_C64 && op->V && !op->v_f32)
+    return fail(NLSE_ERR_ARG, "a complex64 field needs a single-precision potential");
+  StepArgs a = row_args(p, A, op);
+  a.asq = asq;
+  if (asq) a.flags |= F_ASQ_EXT;
+  a.step = (int)step;
+  cudaError_t e = launch_nl_pointwise(p->d.dtype, a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "nonlinear step");
+  return NLSE_OK;
+}
+
+size_t nlse_power_workspace_size(int64_t nseg, int64_t seg_len) {
+  if (nseg <= 0 || seg_len <= 0) return 0;
+  return (size_t)nseg * (size_t)power_chunks(seg_len) * sizeof(double);
+}
+
+int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, double* out,
+               void* workspace, size_t workspace_bytes, void* stream) {
+  g_err.clear();
+  if (!A || !out) return fail(NLSE_ERR_ARG, "null argument");
+  if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
+  if (nseg < 0 || seg_len <= 0) return fail(NLSE_ERR_ARG, "bad segment geometry");
+  const size_t need = nlse_power_workspace_size(nseg, seg_len);
+  if (!workspace || workspace_bytes < need)
+    return fail(NLSE_ERR_ARG, "workspace too small: %zu bytes needed", need);
+  cudaError_t e = launch_power(dtype, A, nseg, seg_len, static_cast<double*>(workspace),
+                               power_chunks(seg_len), out,
+                               reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "power");
+  return NLSE_OK;
+}
+
+int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64_t seg_len,
+                   const double* sums, const double* target, double coef, void* stream) {
+  g_err.clear();
+  if (!in || !out || !sums || !target) return fail(NLSE_ERR_ARG, "null argument");
+  if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
+  cudaError_t e = launch_scale(dtype, in, out, nseg, seg_len, sums, target, coef,
+                               reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "normalize");
+  return NLSE_OK;
+}
+
+int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* stream) {
+  g_err.clear();
+  if (!A || !out) return fail(NLSE_ERR_ARG, "null argument");
+  if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
+  cudaError_t e = launch_abs2(dtype, A, out, n, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "square_mod");
+  return NLSE_OK;
+}
+
+}  // extern "C"

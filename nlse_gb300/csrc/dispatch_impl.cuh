@@ -1,0 +1,106 @@
+// Compile-time-size dispatch of the row and column kernels.  Included by one
+// translation unit per element type (rows_f32.cu, rows_f64.cu, ...), so the
+// template instantiations compile in parallel.
+#pragma once
+#include "launch.h"
+
+namespace nlse {
+
+template <typename F>
+static cudaError_t set_smem(F* kern, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <typename T, int N, int MODE, int NC>
+static cudaError_t rows_n(const StepArgs& a, cudaStream_t s, bool prep) {
+  constexpr int E = Shape<N>::E;
+  using Cfg = RowCfg<N, E>;
+  const size_t smem = size_t(Cfg::LPB) * Cfg::SL * sizeof(cpx<T>);
+  auto kern = k_rows<T, N, E, MODE, NC>;
+  if (prep) return set_smem(kern, smem);
+  const int64_t per_block = Cfg::LPB / NC;
+  const int64_t nblocks = (a.nq + per_block - 1) / per_block;
+  if (nblocks <= 0) return cudaSuccess;
+  kern<<<(unsigned)nblocks, Cfg::THREADS, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int MODE, int NC>
+static cudaError_t rows_mode(int log2n, const StepArgs& a, cudaStream_t s, bool prep) {
+  switch (log2n) {
+    case 1: return rows_n<T, 2, MODE, NC>(a, s, prep);
+    case 2: return rows_n<T, 4, MODE, NC>(a, s, prep);
+    case 3: return rows_n<T, 8, MODE, NC>(a, s, prep);
+    case 4: return rows_n<T, 16, MODE, NC>(a, s, prep);
+    case 5: return rows_n<T, 32, MODE, NC>(a, s, prep);
+    case 6: return rows_n<T, 64, MODE, NC>(a, s, prep);
+    case 7: return rows_n<T, 128, MODE, NC>(a, s, prep);
+    case 8: return rows_n<T, 256, MODE, NC>(a, s, prep);
+    case 9: return rows_n<T, 512, MODE, NC>(a, s, prep);
+    case 10: return rows_n<T, 1024, MODE, NC>(a, s, prep);
+    case 11: return rows_n<T, 2048, MODE, NC>(a, s, prep);
+    case 12: return rows_n<T, 4096, MODE, NC>(a, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// NC = 1: all modes; NC = 2: the modes that apply the nonlinear operator.
+template <typename T, int NC>
+static cudaError_t rows_dispatch(int mode, int log2n, const StepArgs& a, cudaStream_t s, bool prep) {
+  switch (mode) {
+    case ROW_FWD: return rows_mode<T, ROW_FWD, NC>(log2n, a, s, prep);
+    case ROW_INV_NL: return rows_mode<T, ROW_INV_NL, NC>(log2n, a, s, prep);
+    case ROW_INV_NL_FWD: return rows_mode<T, ROW_INV_NL_FWD, NC>(log2n, a, s, prep);
+    case ROW_FULL: return rows_mode<T, ROW_FULL, NC>(log2n, a, s, prep);
+    case ROW_INV:
+      if constexpr (NC == 1) return rows_mode<T, ROW_INV, 1>(log2n, a, s, prep);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T, int N, int MODE>
+static cudaError_t cols_n(const ColArgs& a, cudaStream_t s, bool prep) {
+  constexpr int E = Shape<N>::E;
+  constexpr int TPL = N / E;
+  const int w = prep ? (kColMaxThreads / TPL > 0 ? kColMaxThreads / TPL : 1) : a.w;
+  const size_t smem = size_t(padded_len(N)) * w * sizeof(cpx<T>);
+  auto kern = k_cols<T, N, E, MODE>;
+  if (prep) return set_smem(kern, smem);
+  if (w * TPL > kColMaxThreads) return cudaErrorInvalidConfiguration;
+  if (a.nblocks <= 0) return cudaSuccess;
+  kern<<<(unsigned)a.nblocks, w * TPL, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int MODE>
+static cudaError_t cols_mode(int log2n, const ColArgs& a, cudaStream_t s, bool prep) {
+  switch (log2n) {
+    case 1: return cols_n<T, 2, MODE>(a, s, prep);
+    case 2: return cols_n<T, 4, MODE>(a, s, prep);
+    case 3: return cols_n<T, 8, MODE>(a, s, prep);
+    case 4: return cols_n<T, 16, MODE>(a, s, prep);
+    case 5: return cols_n<T, 32, MODE>(a, s, prep);
+    case 6: return cols_n<T, 64, MODE>(a, s, prep);
+    case 7: return cols_n<T, 128, MODE>(a, s, prep);
+    case 8: return cols_n<T, 256, MODE>(a, s, prep);
+    case 9: return cols_n<T, 512, MODE>(a, s, prep);
+    case 10: return cols_n<T, 1024, MODE>(a, s, prep);
+    case 11: return cols_n<T, 2048, MODE>(a, s, prep);
+    case 12: return cols_n<T, 4096, MODE>(a, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+static cudaError_t cols_dispatch(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prep) {
+  switch (mode) {
+    case COL_FWD: return cols_mode<T, COL_FWD>(log2n, a, s, prep);
+    case COL_INV: return cols_mode<T, COL_INV>(log2n, a, s, prep);
+    case COL_FWD_PROP_INV: return cols_mode<T, COL_FWD_PROP_INV>(log2n, a, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace nlse

@@ -1,0 +1,217 @@
+// In-CTA Stockham FFT building blocks for sm_103a.
+//
+// A "line" is one 1-D transform of power-of-two length N.  The line is held
+// by TPL = N / E threads, each owning E elements in registers.  Thread t owns
+// the elements at positions t + j*TPL (j = 0..E-1) both before the first pass
+// and after the last pass, so global loads and stores of a line are coalesced
+// across consecutive threads and no shared-memory exchange is needed at
+// either end of the transform.  Between radix passes the elements are
+// scattered to their Stockham positions in shared memory and gathered back
+// in the t + j*TPL pattern (P passes need P-1 exchanges).
+//
+// Radix order: radix-16 passes first, the remaining radix (2, 4 or 8) last,
+// so that the small-stride scatter happens when the span NS is large.
+// Shared-memory index padding: one spare slot per 16 elements (padi), which
+// makes both the strided scatter of the first pass and the gathers
+// conflict-free for 8- and 16-byte elements.
+//
+// Twiddles come from one table w[m] = exp(-2*pi*i*m/NMAX) built on the host
+// in FP64 (rounded once to the element type), indexed with stride NMAX/N.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nlse {
+
+constexpr int kLog2NMax = 14;          // largest in-CTA line: 16384 points
+constexpr int kNMax = 1 << kLog2NMax;
+
+template <typename T> struct CT;
+template <> struct CT<float> { using t = float2; };
+template <> struct CT<double> { using t = double2; };
+template <typename T> using cpx = typename CT<T>::t;
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mk(T x, T y) {
+  cpx<T> r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cadd(cpx<T> a, cpx<T> b) {
+  return mk<T>(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> csub(cpx<T> a, cpx<T> b) {
+  return mk<T>(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cscale(cpx<T> a, T s) {
+  return mk<T>(a.x * s, a.y * s);
+}
+// a * (-i) for the forward transform, a * (+i) for the inverse.
+template <typename T, bool INV>
+__device__ __forceinline__ cpx<T> mul_mi(cpx<T> a) {
+  return INV ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);
+}
+// a * w where w = (wr, -wi) forward (exp(-i*theta)), (wr, +wi) inverse.
+template <typename T, bool INV>
+__device__ __forceinline__ cpx<T> mul_w(cpx<T> a, T wr, T wi) {
+  const T s = INV ? wi : -wi;
+  return mk<T>(a.x * wr - a.y * s, a.x * s + a.y * wr);
+}
+
+// cos(pi/8), sin(pi/8), sqrt(1/2)
+#define NLSE_C8 0.92387953251128675613
+#define NLSE_S8 0.38268343236508977173
+#define NLSE_R2 0.70710678118654752440
+
+template <typename T, int R, bool INV> struct DFT;
+
+template <typename T, bool INV> struct DFT<T, 1, INV> {
+  __device__ __forceinline__ static void run(cpx<T>*) {}
+};
+
+template <typename T, bool INV> struct DFT<T, 2, INV> {
+  __device__ __forceinline__ static void run(cpx<T>* x) {
+    const cpx<T> a = x[0], b = x[1];
+    x[0] = cadd<T>(a, b);
+    x[1] = csub<T>(a, b);
+  }
+};
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft4(cpx<T>& a0, cpx<T>& a1, cpx<T>& a2, cpx<T>& a3) {
+  const cpx<T> t0 = cadd<T>(a0, a2), t1 = csub<T>(a0, a2);
+  const cpx<T> t2 = cadd<T>(a1, a3), t3 = mul_mi<T, INV>(csub<T>(a1, a3));
+  a0 = cadd<T>(t0, t2);
+  a1 = cadd<T>(t1, t3);
+  a2 = csub<T>(t0, t2);
+  a3 = csub<T>(t1, t3);
+}
+
+template <typename T, bool INV> struct DFT<T, 4, INV> {
+  __device__ __forceinline__ static void run(cpx<T>* x) { dft4<T, INV>(x[0], x[1], x[2], x[3]); }
+};
+
+template <typename T, bool INV> struct DFT<T, 8, INV> {
+  __device__ __forceinline__ static void run(cpx<T>* x) {
+    cpx<T> e0 = x[0], e1 = x[2], e2 = x[4], e3 = x[6];
+    cpx<T> o0 = x[1], o1 = x[3], o2 = x[5], o3 = x[7];
+    dft4<T, INV>(e0, e1, e2, e3);
+    dft4<T, INV>(o0, o1, o2, o3);
+    const T r = T(NLSE_R2);
+    o1 = mul_w<T, INV>(o1, r, r);
+    o2 = mul_mi<T, INV>(o2);
+    o3 = mul_w<T, INV>(o3, -r, r);
+    x[0] = cadd<T>(e0, o0);
+    x[4] = csub<T>(e0, o0);
+    x[1] = cadd<T>(e1, o1);
+    x[5] = csub<T>(e1, o1);
+    x[2] = cadd<T>(e2, o2);
+    x[6] = csub<T>(e2, o2);
+    x[3] = cadd<T>(e3, o3);
+    x[7] = csub<T>(e3, o3);
+  }
+};
+
+// 16-point DFT as 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2.
+template <typename T, bool INV> struct DFT<T, 16, INV> {
+  __device__ __forceinline__ static void run(cpx<T>* x) {
+    const T c8 = T(NLSE_C8), s8 = T(NLSE_S8), r2 = T(NLSE_R2);
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4<T, INV>(x[n2], x[4 + n2], x[8 + n2], x[12 + n2]);
+    // x[n2 + 4*k1] now holds X[n2][k1]; apply W16^(n2*k1)
+    x[1 + 4 * 1] = mul_w<T, INV>(x[1 + 4 * 1], c8, s8);    // W^1
+    x[1 + 4 * 2] = mul_w<T, INV>(x[1 + 4 * 2], r2, r2);    // W^2
+    x[1 + 4 * 3] = mul_w<T, INV>(x[1 + 4 * 3], s8, c8);    // W^3
+    x[2 + 4 * 1] = mul_w<T, INV>(x[2 + 4 * 1], r2, r2);    // W^2
+    x[2 + 4 * 2] = mul_mi<T, INV>(x[2 + 4 * 2]);           // W^4
+    x[2 + 4 * 3] = mul_w<T, INV>(x[2 + 4 * 3], -r2, r2);   // W^6
+    x[3 + 4 * 1] = mul_w<T, INV>(x[3 + 4 * 1], s8, c8);    // W^3
+    x[3 + 4 * 2] = mul_w<T, INV>(x[3 + 4 * 2], -r2, r2);   // W^6
+    x[3 + 4 * 3] = mul_w<T, INV>(x[3 + 4 * 3], -c8, -s8);  // W^9
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+      dft4<T, INV>(x[4 * k1 + 0], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
+    // x[4*k1 + k2] holds y[k1 + 4*k2]; transpose the 4x4 index in registers.
+    cpx<T> y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) y[k1 + 4 * k2] = x[4 * k1 + k2];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = y[i];
+  }
+};
+
+__host__ __device__ constexpr int padi(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_len(int n) { return padi(n - 1) + 1; }
+
+// Elements per thread and threads per line for an N-point line.
+template <int N, int EREQ = 16> struct Shape {
+  static constexpr int E = N >= EREQ ? EREQ : N;
+  static constexpr int TPL = N / E;
+};
+
+// One radix-R Stockham pass over the thread's E elements.  On entry x[j]
+// holds input position t + j*TPL; element j = s + r*BPT is input r of
+// butterfly b = t + s*TPL.  On exit x[s + r*BPT] holds output position
+// (b / NS) * NS * R + (b % NS) + r * NS.
+template <typename T, int N, int E, int R, int NS, bool INV>
+__device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T>* __restrict__ tw) {
+  constexpr int TPL = N / E, BPT = E / R;
+  constexpr int TWS = kNMax / N * (N / (NS * R));  // table stride per unit of r*k
+#pragma unroll
+  for (int s = 0; s < BPT; ++s) {
+    cpx<T> y[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) y[r] = x[s + r * BPT];
+    if constexpr (NS > 1) {
+      const int k = (t + s * TPL) & (NS - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        cpx<T> w = __ldg(&tw[(r * k) * TWS]);
+        if (INV) w.y = -w.y;
+        y[r] = cmul<T>(y[r], w);
+      }
+    }
+    DFT<T, R, INV>::run(y);
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[s + r * BPT] = y[r];
+  }
+}
+
+// Full N-point transform of one line.  sm points at the line's padded shared
+// buffer; element i lives at sm[padi(i) * STRIDE] (STRIDE > 1 interleaves W
+// column lines, the caller offsets sm by the column).  All threads of the
+// CTA must call this (it contains __syncthreads).
+template <typename T, int N, int E, int NS, bool INV>
+__device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
+                                         const cpx<T>* __restrict__ tw) {
+  constexpr int TPL = N / E;
+  constexpr int R = (N / NS) >= 16 ? 16 : (N / NS);
+  constexpr int BPT = E / R;
+  stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
+  if constexpr (NS * R < N) {
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < BPT; ++s) {
+      const int b = t + s * TPL;
+      const int base = (b / NS) * NS * R + (b & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[padi(base + r * NS) * stride] = x[s + r * BPT];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sm[padi(t + j * TPL) * stride];
+    fft_line<T, N, E, NS * R, INV>(x, t, sm, stride, tw);
+  }
+}
+
+}  // namespace nlse

@@ -1,0 +1,32 @@
+// Host-side launchers shared by the translation units of libnlse_sm103.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "step_kernels.cuh"
+
+namespace nlse {
+
+constexpr int kMinLog2 = 1;   // smallest line: 2 points
+constexpr int kMaxLog2 = 12;  // largest line handled by one CTA: 4096 points
+
+// Row passes (contiguous axis).  prepare_only: set kernel attributes, launch
+// nothing (done once per device before any stream capture).
+cudaError_t launch_rows_f32_c1(int mode, int log2n, const StepArgs& a, cudaStream_t s, bool prepare_only);
+cudaError_t launch_rows_f32_c2(int mode, int log2n, const StepArgs& a, cudaStream_t s, bool prepare_only);
+cudaError_t launch_rows_f64_c1(int mode, int log2n, const StepArgs& a, cudaStream_t s, bool prepare_only);
+cudaError_t launch_rows_f64_c2(int mode, int log2n, const StepArgs& a, cudaStream_t s, bool prepare_only);
+// Column passes (strided axis).
+cudaError_t launch_cols_f32(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
+cudaError_t launch_cols_f64(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
+
+// Pointwise kernels (pointwise.cu).
+int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction
+cudaError_t launch_power(int dtype, const void* A, int64_t nseg, int64_t seg_len, double* partial,
+                         int nchunks, double* out, cudaStream_t s);
+cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int64_t seg_len,
+                         const double* sums, const double* target, double coef, cudaStream_t s);
+cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStream_t s);
+
+}  // namespace nlse

@@ -1,0 +1,201 @@
+// Pointwise and reduction kernels: FP64 power sums, power normalisation,
+// the standalone nonlinear operator and |A|^2.
+#include "launch.h"
+
+namespace nlse {
+
+constexpr int kRedThreads = 256;
+constexpr int64_t kRedChunk = 8192;  // elements reduced by one block
+
+int power_chunks(int64_t seg_len) {
+  int64_t c = (seg_len + kRedChunk - 1) / kRedChunk;
+  if (c < 1) c = 1;
+  if (c > 1024) c = 1024;
+  return (int)c;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block (chunk, seg) sums |A|^2 over its slice of segment seg in FP64 and
+// writes one partial; the final pass adds the partials of a segment in a
+// fixed order, so the result does not depend on scheduling.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_power_partial(const cpx<T>* __restrict__ A,
+                                                               int64_t seg_len, int nchunks,
+                                                               double* __restrict__ partial) {
+  const int64_t seg = blockIdx.y;
+  const int chunk = blockIdx.x;
+  const int64_t clen = (seg_len + nchunks - 1) / nchunks;
+  const int64_t lo = chunk * clen;
+  const int64_t hi = lo + clen < seg_len ? lo + clen : seg_len;
+  const cpx<T>* a = A + seg * seg_len;
+  double acc = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
+    const cpx<T> v = a[i];
+    const double x = double(v.x), y = double(v.y);
+    acc += x * x + y * y;
+  }
+  __shared__ double ws[kRedThreads / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < kRedThreads / 32 ? ws[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[seg * nchunks + chunk] = v;
+  }
+}
+
+__global__ void k_power_final(const double* __restrict__ partial, int nchunks, int64_t nseg,
+                              double* __restrict__ out) {
+  const int64_t seg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (seg >= nseg) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunks; ++c) s += partial[seg * nchunks + c];
+  out[seg] = s;
+}
+
+template <typename T>
+__global__ void k_scale(const cpx<T>* __restrict__ in, cpx<T>* __restrict__ out, int64_t seg_len,
+                        int64_t total, const double* __restrict__ sums,
+                        const double* __restrict__ target, double coef) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t seg = i / seg_len;
+    const T s = T(sqrt(target[seg] / (sums[seg] * coef)));
+    const cpx<T> v = in[i];
+    out[i] = mk<T>(v.x * s, v.y * s);
+  }
+}
+
+template <typename T>
+__global__ void k_abs2(const cpx<T>* __restrict__ A, T* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = abs2<T>(A[i]);
+}
+
+// Nonlinear step of parameter set 0 on every pixel; one thread owns all the
+// components of a pixel.
+template <typename T, int NC>
+__global__ void k_nl_point(const StepArgs a) {
+  const int64_t total = (a.nq / a.lines_per_comp) * a.pix;
+  cpx<T>* A = reinterpret_cast<cpx<T>*>(a.A);
+  const T* asq = reinterpret_cast<const T*>(a.asq);
+  const bool has_v = a.flags & F_HAS_V;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / a.pix, px = i % a.pix;
+    const double* P = a.params + f * kParamStride;
+    const int64_t i0 = (f * NC) * a.pix + px;
+    const cpx<T> x0 = A[i0];
+    T a0 = (a.flags & F_ASQ_EXT) ? asq[i0] : abs2<T>(x0);
+    const NLP<T> p0 = load_nlp<T>(P);
+    const int64_t vi = f * a.v_fstride + px;
+    const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
+    if constexpr (NC == 1) {
+      A[i0] = nl_point<T>(x0, a0, T(0), p0, has_v, v0);
+    } else {
+      const int64_t i1 = i0 + a.pix;
+      const cpx<T> x1 = A[i1];
+      const T a1 = (a.flags & F_ASQ_EXT) ? asq[i1] : abs2<T>(x1);
+      const NLP<T> p1 = load_nlp<T>(P + 7);
+      const cpx<T> v1 = has_v ? load_vp<T>(a.V, a.flags, vi, p1.vs) : mk<T>(T(0), T(0));
+      cpx<T> y0 = nl_point<T>(x0, a0, a1, p0, has_v, v0);
+      cpx<T> y1 = nl_point<T>(x1, a1, a0, p1, has_v, v1);
+      if (a.flags & F_RABI) {
+        const T rc = T(P[14]), rs = T(P[15]);
+        const cpx<T> z0 = mk<T>(rc * y0.x + rs * y1.y, rc * y0.y - rs * y1.x);
+        const cpx<T> z1 = mk<T>(rc * y1.x + rs * y0.y, rc * y1.y - rs * y0.x);
+        y0 = z0;
+        y1 = z1;
+      }
+      if (a.flags & (F_PUMP | F_PROBE)) {
+        const T dz = T(P[30]);
+        if (a.flags & F_PUMP) {
+          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[px],
+                             reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]);
+          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
+        }
+        if (a.flags & F_PROBE) {
+          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.probe_r)[px],
+                             reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]);
+          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
+        }
+      }
+      A[i0] = y0;
+      A[i1] = y1;
+    }
+  }
+}
+
+static unsigned grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g > 152 * 32) g = 152 * 32;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+cudaError_t launch_power(int dtype, const void* A, int64_t nseg, int64_t seg_len, double* partial,
+                         int nchunks, double* out, cudaStream_t s) {
+  if (nseg <= 0) return cudaSuccess;
+  const dim3 grid(nchunks, (unsigned)nseg);
+  if (dtype == 0)
+    k_power_partial<float><<<grid, kRedThreads, 0, s>>>(reinterpret_cast<const float2*>(A), seg_len,
+                                                         nchunks, partial);
+  else
+    k_power_partial<double><<<grid, kRedThreads, 0, s>>>(reinterpret_cast<const double2*>(A),
+                                                          seg_len, nchunks, partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_power_final<<<(unsigned)((nseg + 127) / 128), 128, 0, s>>>(partial, nchunks, nseg, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int64_t seg_len,
+                         const double* sums, const double* target, double coef, cudaStream_t s) {
+  const int64_t total = nseg * seg_len;
+  if (total <= 0) return cudaSuccess;
+  if (dtype == 0)
+    k_scale<float><<<grid_for(total, 256), 256, 0, s>>>(reinterpret_cast<const float2*>(in),
+                                                        reinterpret_cast<float2*>(out), seg_len,
+                                                        total, sums, target, coef);
+  else
+    k_scale<double><<<grid_for(total, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(in),
+                                                         reinterpret_cast<double2*>(out), seg_len,
+                                                         total, sums, target, coef);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (dtype == 0)
+    k_abs2<float><<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const float2*>(A),
+                                                   reinterpret_cast<float*>(out), n);
+  else
+    k_abs2<double><<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(A),
+                                                    reinterpret_cast<double*>(out), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s) {
+  const int64_t total = (a.nq / a.lines_per_comp) * a.pix;
+  if (total <= 0) return cudaSuccess;
+  const unsigned g = grid_for(total, 256);
+  if (dtype == 0) {
+    if (a.comps == 1) k_nl_point<float, 1><<<g, 256, 0, s>>>(a);
+    else k_nl_point<float, 2><<<g, 256, 0, s>>>(a);
+  } else {
+    if (a.comps == 1) k_nl_point<double, 1><<<g, 256, 0, s>>>(a);
+    else k_nl_point<double, 2><<<g, 256, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace nlse

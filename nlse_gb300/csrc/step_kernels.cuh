@@ -1,0 +1,376 @@
+// Split-step kernels: row passes (contiguous axis), column passes (strided
+// axes) and the pointwise nonlinear operator fused into them.
+//
+// The arithmetic of the nonlinear operator follows the GPU kernels of the
+// reference package (NLSE/kernels_gpu.py):
+//   nl_prop            kernels_gpu.py:4-35
+//   nl_prop_without_V  kernels_gpu.py:38-65
+//   nl_prop_c          kernels_gpu.py:68-104
+//   nl_prop_without_V_c kernels_gpu.py:107-139
+//   rabi_coupling      kernels_gpu.py:142-156
+// and the DDGPE pump callback (NLSE/ddgpe.py:127-156).  All of them are one
+// formula here: a single-component field is the two-component formula with
+// the cross terms set to g12 = 0, Isat2 = inf, |A2|^2 = 0, which adds exact
+// zeros.
+#pragma once
+#include "fft_core.cuh"
+
+namespace nlse {
+
+// ---- parameters -----------------------------------------------------------
+// Per-field parameter block, 32 doubles (filled by the host, see capi.cu):
+//   [set*16 + comp*7 + k]   set 0 = after the linear step, set 1 = before it
+//                            (Strang "double" scheme); k = dz, alpha, g_self,
+//                            g_cross, isat_self, isat_cross, vscale
+//   [14], [15]              Rabi cos(omega*dz), sin(omega*dz)
+//   [30]                    dz used by the pump term
+constexpr int kParamStride = 32;
+
+enum : uint32_t {
+  F_HAS_V = 1u << 0,      // potential present
+  F_V_COMPLEX = 1u << 1,  // potential stored complex (else real)
+  F_PROP_C128 = 1u << 2,  // propagator stored as complex128
+  F_RABI = 1u << 3,       // Rabi rotation after the nonlinear step
+  F_PUMP = 1u << 4,       // DDGPE pump term on component 1
+  F_PROBE = 1u << 5,      // DDGPE probe term on component 1
+  F_PRE_NL = 1u << 6,     // nonlinear half step before the linear step
+  F_ASQ_EXT = 1u << 7,    // |A|^2 read from the external (convolved) buffer
+  F_NO_POST = 1u << 8,    // skip the post-linear nonlinear step (plain FFT use)
+  F_V_F32 = 1u << 9,      // potential stored in single precision: V' = vscale*V is
+                          // formed in FP32 and then widened, as the reference does
+                          // for a complex64 V with a complex128 field
+};
+
+struct StepArgs {
+  void* A;                  // field, complex T, in place
+  const void* V;            // potential: T or cpx<T>, null if absent
+  const void* prop;         // propagator: cpx<float> or cpx<double>
+  const double* params;     // [nfields][32]
+  const void* pump_r;       // cpx<T> [pixels]
+  const void* pump_t;       // cpx<T> [steps]
+  const void* probe_r;
+  const void* probe_t;
+  const void* asq;          // T [nfields][comps][pixels] (nonlocal |A|^2), or null
+  const void* tw;           // twiddle table cpx<T> [kNMax]
+  int64_t nq;               // pixel-lines (fields * lines_per_comp)
+  int64_t lines_per_comp;   // lines of one component of one field
+  int64_t pix;              // pixels of one component of one field
+  int64_t v_fstride;        // field stride of V (0: shared)
+  int64_t prop_cstride;     // component stride of the propagator
+  double inv_n;             // 1 / (number of pixels), inverse-FFT normalisation
+  int comps;                // 1 or 2
+  int step;                 // step index (pump time profile)
+  int nsteps;               // steps fused inside one launch (1-D full mode)
+  uint32_t flags;
+};
+
+struct ColArgs {
+  void* A;
+  const void* prop;
+  const void* tw;
+  int64_t nblocks;          // column blocks * outer
+  int64_t ncb;              // column blocks per outer slab
+  int64_t outer_stride;     // elements between outer slabs
+  int64_t ld;               // elements between consecutive points of a column
+  int64_t prop_cstride;
+  int comps;                // outer index % comps selects the propagator component
+  int w;                    // columns per block (power of two)
+  uint32_t flags;
+};
+
+template <typename T> struct NLP {
+  T dz, alpha, gs, gc, is, ic;
+  double vs;
+};
+
+template <typename T>
+__device__ __forceinline__ NLP<T> load_nlp(const double* __restrict__ p) {
+  NLP<T> r;
+  r.dz = T(__ldg(p + 0));
+  r.alpha = T(__ldg(p + 1));
+  r.gs = T(__ldg(p + 2));
+  r.gc = T(__ldg(p + 3));
+  r.is = T(__ldg(p + 4));
+  r.ic = T(__ldg(p + 5));
+  r.vs = __ldg(p + 6);
+  return r;
+}
+
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ float exp_t(float x) { return expf(x); }
+__device__ __forceinline__ double exp_t(double x) { return exp(x); }
+
+// One nonlinear sub-step on one point (kernels_gpu.py:68-104 form):
+//   sat = 1 / (1 + a_s/Isat_s + a_c/Isat_c)
+//   arg = i*(g_s*a_s*sat + g_c*a_c*sat) - alpha*sat + i*V',  V' = vscale*V
+//   A  *= exp(dz*arg)
+template <typename T>
+__device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>& p, bool has_v,
+                                           cpx<T> vp) {
+  const T sat = T(1) / (T(1) + a_s / p.is + a_c / p.ic);
+  T im = p.gs * a_s * sat + p.gc * a_c * sat;
+  T re = -p.alpha * sat;
+  if (has_v) {
+    // arg += 1j * V'  ->  (re - Im V', im + Re V')
+    re = re - vp.y;
+    im = im + vp.x;
+  }
+  re = mul_rn(re, p.dz);
+  im = mul_rn(im, p.dz);
+  const T e = exp_t(re);
+  T s, c;
+  sincos_t(im, &s, &c);
+  return cmul<T>(A, mk<T>(e * c, e * s));
+}
+
+template <typename T>
+__device__ __forceinline__ T abs2(cpx<T> a) {
+  return a.x * a.x + a.y * a.y;
+}
+
+// V' = vscale * V rounded the way the reference rounds its k/2*V array: in
+// the storage precision of V, then widened to the field precision.
+template <typename T>
+__device__ __forceinline__ cpx<T> load_vp(const void* V, uint32_t flags, int64_t idx, double vs) {
+  if (flags & F_V_F32) {
+    const float fs = float(vs);
+    float2 v;
+    if (flags & F_V_COMPLEX) v = __ldg(reinterpret_cast<const float2*>(V) + idx);
+    else v = make_float2(__ldg(reinterpret_cast<const float*>(V) + idx), 0.f);
+    return mk<T>(T(__fmul_rn(fs, v.x)), T(__fmul_rn(fs, v.y)));
+  }
+  double2 v;
+  if (flags & F_V_COMPLEX) v = __ldg(reinterpret_cast<const double2*>(V) + idx);
+  else v = make_double2(__ldg(reinterpret_cast<const double*>(V) + idx), 0.0);
+  return mk<T>(T(__dmul_rn(vs, v.x)), T(__dmul_rn(vs, v.y)));
+}
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mul_prop(cpx<T> x, const void* prop, uint32_t flags, int64_t idx);
+
+template <>
+__device__ __forceinline__ float2 mul_prop<float>(float2 x, const void* prop, uint32_t flags,
+                                                  int64_t idx) {
+  if (flags & F_PROP_C128) {
+    // complex64 field times complex128 propagator: product in FP64, rounded
+    const double2 p = __ldg(reinterpret_cast<const double2*>(prop) + idx);
+    const double xr = x.x, xi = x.y;
+    return make_float2(float(xr * p.x - xi * p.y), float(xr * p.y + xi * p.x));
+  }
+  const float2 p = __ldg(reinterpret_cast<const float2*>(prop) + idx);
+  return cmul<float>(x, p);
+}
+
+template <>
+__device__ __forceinline__ double2 mul_prop<double>(double2 x, const void* prop, uint32_t flags,
+                                                    int64_t idx) {
+  if (flags & F_PROP_C128) return cmul<double>(x, __ldg(reinterpret_cast<const double2*>(prop) + idx));
+  const float2 p = __ldg(reinterpret_cast<const float2*>(prop) + idx);
+  return cmul<double>(x, make_double2(double(p.x), double(p.y)));
+}
+
+// Nonlinear step (set 0 or 1) for the E points a thread owns of one line.
+// x: own component, xo: partner component (two-component models only, same
+// positions).  pix0: pixel index of position t within the component, the
+// thread's points are pix0 + j*TPL.
+template <typename T, int E, int TPL, int NC>
+__device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], const StepArgs& a,
+                                        int64_t f, int comp, int64_t pix0, int set, bool post) {
+  const double* P = a.params + f * kParamStride + set * 16;
+  const NLP<T> ps = load_nlp<T>(P + comp * 7);
+  constexpr bool two = NC == 2;
+  const bool rabi = two && post && (a.flags & F_RABI);
+  NLP<T> po;
+  if (rabi) po = load_nlp<T>(P + (1 - comp) * 7);
+  const bool has_v = a.flags & F_HAS_V;
+  const int64_t vb = f * a.v_fstride + pix0;
+  const T* asq = reinterpret_cast<const T*>(a.asq);
+  const int64_t qb_s = (f * NC + comp) * a.pix + pix0;
+  const int64_t qb_o = (f * NC + (1 - comp)) * a.pix + pix0;
+  T rc = T(0), rs = T(0);
+  if (rabi) {
+    rc = T(__ldg(a.params + f * kParamStride + 14));
+    rs = T(__ldg(a.params + f * kParamStride + 15));
+  }
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    T as, ao = T(0);
+    if (a.flags & F_ASQ_EXT) {
+      as = asq[qb_s + j * TPL];
+      if (two) ao = asq[qb_o + j * TPL];
+    } else {
+      as = abs2<T>(x[j]);
+      if (two) ao = abs2<T>(xo[j]);
+    }
+    const cpx<T> v = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, ps.vs) : mk<T>(T(0), T(0));
+    cpx<T> y = nl_point<T>(x[j], as, ao, ps, has_v, v);
+    if (two && rabi) {
+      // kernels_gpu.py:154-156: A1' = cos*A1 - i*sin*A2, A2' = cos*A2 - i*sin*A1
+      const cpx<T> vo = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, po.vs) : mk<T>(T(0), T(0));
+      const cpx<T> yo = nl_point<T>(xo[j], ao, as, po, has_v, vo);
+      y = mk<T>(rc * y.x + rs * yo.y, rc * y.y - rs * yo.x);
+    }
+    x[j] = y;
+  }
+  if (two && post && comp == 1 && (a.flags & (F_PUMP | F_PROBE))) {
+    // ddgpe.py:155-156: A2 -= F_r * F_t[i] * dz * 1j  (pump, then probe)
+    const T dz = T(__ldg(a.params + f * kParamStride + 30));
+    const cpx<T>* pr = reinterpret_cast<const cpx<T>*>(a.pump_r);
+    const cpx<T>* qr = reinterpret_cast<const cpx<T>*>(a.probe_r);
+    const cpx<T> ptv = (a.flags & F_PUMP) ? reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]
+                                          : mk<T>(T(0), T(0));
+    const cpx<T> qtv = (a.flags & F_PROBE) ? reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]
+                                           : mk<T>(T(0), T(0));
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      if (a.flags & F_PUMP) {
+        cpx<T> u = cmul<T>(pr[pix0 + j * TPL], ptv);
+        u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+        x[j] = mk<T>(x[j].x + u.y, x[j].y - u.x);
+      }
+      if (a.flags & F_PROBE) {
+        cpx<T> u = cmul<T>(qr[pix0 + j * TPL], qtv);
+        u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+        x[j] = mk<T>(x[j].x + u.y, x[j].y - u.x);
+      }
+    }
+  }
+}
+
+// ---- row kernels ----------------------------------------------------------
+enum RowMode : int {
+  ROW_FWD = 0,         // [pre-NL] forward FFT
+  ROW_INV_NL = 1,      // inverse FFT, 1/N, post-NL [Rabi, pump]
+  ROW_INV_NL_FWD = 2,  // ROW_INV_NL, then [pre-NL] and the next forward FFT
+  ROW_FULL = 3,        // 1-D: [pre-NL] FFT, propagator, iFFT, 1/N, post-NL; nsteps times
+  ROW_INV = 4,         // inverse FFT with 1/N only
+};
+
+template <int N, int E> struct RowCfg {
+  static constexpr int TPL = N / E;
+  static constexpr int LPB = (256 / TPL) >= 2 ? 256 / TPL : 2;  // lines per block, even
+  static constexpr int THREADS = LPB * TPL;
+  static constexpr int SL = padded_len(N);
+};
+
+template <typename T, int N, int E>
+__device__ __forceinline__ void exchange_partner(const cpx<T> (&x)[E], cpx<T> (&xo)[E], cpx<T>* sm,
+                                                 int lb, int t) {
+  constexpr int TPL = N / E, SL = RowCfg<N, E>::SL;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < E; ++j) sm[lb * SL + padi(t + j * TPL)] = x[j];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < E; ++j) xo[j] = sm[(lb ^ 1) * SL + padi(t + j * TPL)];
+}
+
+template <typename T, int N, int E, int MODE, int NC>
+__global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a) {
+  using C = cpx<T>;
+  constexpr int TPL = RowCfg<N, E>::TPL, LPB = RowCfg<N, E>::LPB, SL = RowCfg<N, E>::SL;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const int lb = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  constexpr int nc = NC;
+  const int comp = lb % nc;
+  const int64_t q = (int64_t)blockIdx.x * (LPB / nc) + lb / nc;
+  const bool act = q < a.nq;
+  const int64_t qq = act ? q : 0;
+  const int64_t f = qq / a.lines_per_comp, m = qq % a.lines_per_comp;
+  C* A = reinterpret_cast<C*>(a.A) + ((f * nc + comp) * a.lines_per_comp + m) * (int64_t)N;
+  const int64_t pix0 = m * N + t;
+  C* sml = sm + lb * SL;
+  constexpr bool two = NC == 2;
+
+  C x[E], xo[E];
+#pragma unroll
+  for (int j = 0; j < E; ++j) x[j] = act ? A[t + j * TPL] : mk<T>(T(0), T(0));
+
+  if constexpr (MODE == ROW_FWD || MODE == ROW_FULL) {
+    if (a.flags & F_PRE_NL) {
+      if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
+      nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
+    }
+  }
+  const int nsteps = (MODE == ROW_FULL) ? a.nsteps : 1;
+  for (int st = 0; st < nsteps; ++st) {
+    if constexpr (MODE == ROW_FULL) {
+      if (st > 0 && (a.flags & F_PRE_NL)) {
+        if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
+        nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
+      }
+      fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
+      const int64_t pb = comp * a.prop_cstride + t;
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = mul_prop<T>(x[j], a.prop, a.flags, pb + j * TPL);
+    }
+    if constexpr (MODE == ROW_FWD) {
+      fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
+    } else {
+      fft_line<T, N, E, 1, true>(x, t, sml, 1, tw);
+      const T s = T(a.inv_n);
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], s);
+      if constexpr (MODE != ROW_INV) {
+        if (!(a.flags & F_NO_POST)) {
+          if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
+          nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true);
+        }
+      }
+      if constexpr (MODE == ROW_INV_NL_FWD) {
+        if (a.flags & F_PRE_NL) {
+          if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
+          nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
+        }
+        fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
+      }
+    }
+  }
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < E; ++j) A[t + j * TPL] = x[j];
+  }
+}
+
+// ---- column kernels -------------------------------------------------------
+enum ColMode : int {
+  COL_FWD = 0,
+  COL_INV = 1,           // no normalisation (applied by the last row pass)
+  COL_FWD_PROP_INV = 2,  // forward, propagator multiply, inverse
+};
+
+constexpr int kColMaxThreads = 512;
+
+template <typename T, int N, int E, int MODE>
+__global__ void __launch_bounds__(kColMaxThreads) k_cols(const ColArgs a) {
+  using C = cpx<T>;
+  constexpr int TPL = N / E;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const int W = a.w;
+  const int c = threadIdx.x & (W - 1), t = threadIdx.x / W;
+  const int64_t blk = blockIdx.x;
+  const int64_t b = blk % a.ncb, o = blk / a.ncb;
+  C* base = reinterpret_cast<C*>(a.A) + o * a.outer_stride + b * W + c;
+  C x[E];
+#pragma unroll
+  for (int j = 0; j < E; ++j) x[j] = base[(int64_t)(t + j * TPL) * a.ld];
+  fft_line<T, N, E, 1, MODE == COL_INV>(x, t, sm + c, W, tw);
+  if constexpr (MODE == COL_FWD_PROP_INV) {
+    const int64_t pb = (o % a.comps) * a.prop_cstride + b * W + c;
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      x[j] = mul_prop<T>(x[j], a.prop, a.flags, pb + (int64_t)(t + j * TPL) * a.ld);
+    fft_line<T, N, E, 1, true>(x, t, sm + c, W, tw);
+  }
+#pragma unroll
+  for (int j = 0; j < E; ++j) base[(int64_t)(t + j * TPL) * a.ld] = x[j];
+}
+
+}  // namespace nlse

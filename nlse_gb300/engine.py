@@ -1,0 +1,242 @@
+"""Device-side engine: plans, operators and the calls into libnlse_sm103.
+
+Fields and parameters live in torch CUDA tensors owned by Python; the C
+library receives raw pointers and the current CUDA stream.  Nothing here
+computes on the host beyond the small per-field parameter blocks.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_DT = {torch.complex64: _lib.NLSE_C64, torch.complex128: _lib.NLSE_C128}
+
+
+def dtype_code(t: torch.Tensor) -> int:
+    try:
+        return _DT[t.dtype]
+    except KeyError:
+        raise TypeError(f"field dtype must be complex64 or complex128, got {t.dtype}") from None
+
+
+def stream_handle(device: torch.device | None = None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def require_cuda(t: torch.Tensor, name: str = "field") -> None:
+    if not (isinstance(t, torch.Tensor) and t.is_cuda):
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be C-contiguous")
+
+
+class Plan:
+    """A libnlse_sm103 plan for one field geometry (the VkFFTApp analogue)."""
+
+    _cache: dict = {}
+
+    def __init__(self, ndim: int, shape: tuple, nfields: int, comps: int, dtype: int,
+                 device: torch.device):
+        self.lib = _lib.load()
+        self.ndim, self.shape, self.nfields = ndim, tuple(int(s) for s in shape), int(nfields)
+        self.comps, self.dtype, self.device = int(comps), int(dtype), device
+        d = _lib.Desc()
+        d.ndim = ndim
+        for i, s in enumerate(self.shape):
+            d.shape[i] = s
+        d.nfields = self.nfields
+        d.comps = self.comps
+        d.dtype = dtype
+        h = ct.c_void_p()
+        with torch.cuda.device(device):
+            _lib.check(self.lib.nlse_plan_create(ct.byref(h), ct.byref(d)), "plan")
+        self.handle = h
+        self.shape0 = self.shape
+
+    @classmethod
+    def get(cls, ndim, shape, nfields, comps, dtype, device) -> "Plan":
+        key = (ndim, tuple(shape), int(nfields), int(comps), int(dtype), str(device))
+        p = cls._cache.get(key)
+        if p is None:
+            p = cls(ndim, shape, nfields, comps, dtype, device)
+            cls._cache[key] = p
+        return p
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.nlse_plan_destroy(h)
+            except Exception:
+                pass
+
+    # -- transforms -------------------------------------------------------
+    def fft(self, A: torch.Tensor, B: torch.Tensor | None = None) -> torch.Tensor:
+        """Forward transform over the plan axes (VkFFTApp.fft)."""
+        return self._fft(A, B, 0)
+
+    def ifft(self, A: torch.Tensor, B: torch.Tensor | None = None) -> torch.Tensor:
+        """Normalised inverse transform (VkFFTApp.ifft with norm=1)."""
+        return self._fft(A, B, 1)
+
+    def _fft(self, A, B, inverse):
+        require_cuda(A)
+        if B is not None and B.data_ptr() != A.data_ptr():
+            B.copy_(A)
+            A = B
+        with torch.cuda.device(A.device):
+            _lib.check(self.lib.nlse_fft(self.handle, A.data_ptr(), inverse,
+                                         stream_handle(A.device)), "fft")
+        return A
+
+
+@dataclass
+class OperatorData:
+    """Device buffers of one split-step operator and its C descriptor."""
+
+    prop: torch.Tensor
+    params: torch.Tensor
+    scheme: int
+    rabi: bool = False
+    V: torch.Tensor | None = None
+    v_fstride: int = 0
+    prop_cstride: int = 0
+    pump: tuple | None = None  # (pump_r, pump_t, probe_r, probe_t) device tensors or None
+    keep: list = field(default_factory=list)
+
+    def struct(self) -> _lib.Operator:
+        o = _lib.Operator()
+        if self.V is not None:
+            o.V = self.V.data_ptr()
+            o.v_complex = int(self.V.is_complex())
+            o.v_f32 = int(self.V.dtype in (torch.float32, torch.complex64))
+            o.v_fstride = int(self.v_fstride)
+        o.prop = self.prop.data_ptr()
+        o.prop_c128 = int(self.prop.dtype == torch.complex128)
+        o.prop_cstride = int(self.prop_cstride)
+        o.params = self.params.data_ptr()
+        o.scheme = int(self.scheme)
+        o.rabi = int(bool(self.rabi))
+        if self.pump is not None:
+            pr, pt, qr, qt = self.pump
+            if pr is not None:
+                o.pump_r, o.pump_t = pr.data_ptr(), pt.data_ptr()
+            if qr is not None:
+                o.probe_r, o.probe_t = qr.data_ptr(), qt.data_ptr()
+        return o
+
+
+def propagate(plan: Plan, A: torch.Tensor, op: OperatorData, nsteps: int, step0: int = 0,
+              graph: bool = False) -> None:
+    """Advance A in place by nsteps split steps (nlse_propagate)."""
+    require_cuda(A)
+    s = op.struct()
+    flags = _lib.NLSE_RUN_GRAPH if graph else 0
+    with torch.cuda.device(A.device):
+        _lib.check(plan.lib.nlse_propagate(plan.handle, A.data_ptr(), ct.byref(s), int(nsteps),
+                                           int(step0), flags, stream_handle(A.device)),
+                   "propagate")
+
+
+def nonlinear(plan: Plan, A: torch.Tensor, op: OperatorData, asq: torch.Tensor | None = None,
+              step: int = 0) -> None:
+    """Nonlinear step only (parameter set 0), pointwise (nlse_nonlinear)."""
+    require_cuda(A)
+    s = op.struct()
+    with torch.cuda.device(A.device):
+        _lib.check(plan.lib.nlse_nonlinear(plan.handle, A.data_ptr(),
+                                           asq.data_ptr() if asq is not None else None,
+                                           ct.byref(s), int(step), stream_handle(A.device)),
+                   "nonlinear")
+
+
+def power(A: torch.Tensor, nseg: int) -> torch.Tensor:
+    """FP64 sums of |A|^2 over nseg equal contiguous segments (device tensor)."""
+    require_cuda(A)
+    lib = _lib.load()
+    n = A.numel()
+    if nseg <= 0 or n % nseg:
+        raise ValueError("segments must tile the array")
+    seg = n // nseg
+    out = torch.empty(nseg, dtype=torch.float64, device=A.device)
+    wsb = lib.nlse_power_workspace_size(nseg, seg)
+    ws = torch.empty(max(1, wsb // 8), dtype=torch.float64, device=A.device)
+    with torch.cuda.device(A.device):
+        _lib.check(lib.nlse_power(A.data_ptr(), dtype_code(A), nseg, seg, out.data_ptr(),
+                                  ws.data_ptr(), wsb, stream_handle(A.device)), "power")
+    return out
+
+
+def normalize(src: torch.Tensor, dst: torch.Tensor, nseg: int, sums: torch.Tensor,
+              target: torch.Tensor, coef: float) -> None:
+    """dst = src * sqrt(target / (sums * coef)) per segment (nlse_normalize)."""
+    require_cuda(src)
+    require_cuda(dst)
+    lib = _lib.load()
+    seg = src.numel() // nseg
+    with torch.cuda.device(src.device):
+        _lib.check(lib.nlse_normalize(src.data_ptr(), dst.data_ptr(), dtype_code(src), nseg, seg,
+                                      sums.data_ptr(), target.data_ptr(), float(coef),
+                                      stream_handle(src.device)), "normalize")
+
+
+def square_mod(A: torch.Tensor, out: torch.Tensor) -> None:
+    require_cuda(A)
+    require_cuda(out)
+    lib = _lib.load()
+    with torch.cuda.device(A.device):
+        _lib.check(lib.nlse_square_mod(A.data_ptr(), out.data_ptr(), dtype_code(A), A.numel(),
+                                       stream_handle(A.device)), "square_mod")
+
+
+def per_field(x, lead: tuple, n_axes: int, name: str) -> np.ndarray:
+    """Broadcast a scalar or per-field parameter to one float64 value per field.
+
+    The reference broadcasts parameter arrays against the field with NumPy
+    rules; per-field values are arrays whose trailing n_axes dimensions are 1
+    (e.g. n2 of shape (B, 1, 1) for (B, NY, NX) fields).
+    """
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().numpy()
+    a = np.asarray(x)
+    if np.iscomplexobj(a):
+        if np.any(a.imag != 0):
+            raise NotImplementedError(f"complex {name} is not supported")
+        a = a.real
+    a = a.astype(np.float64)
+    if a.ndim > 0:
+        if a.ndim >= n_axes and n_axes > 0:
+            tail = a.shape[a.ndim - n_axes:]
+            if any(t != 1 for t in tail):
+                raise NotImplementedError(
+                    f"{name} varies across the transverse grid (shape {a.shape}); only per-field "
+                    "values with trailing singleton axes are supported")
+            a = a.reshape(a.shape[: a.ndim - n_axes])
+        elif n_axes > 0:
+            raise NotImplementedError(
+                f"{name} of shape {a.shape} would broadcast along the grid axes")
+    try:
+        b = np.broadcast_to(a, lead)
+    except ValueError:
+        raise ValueError(f"{name} of shape {np.shape(x)} does not broadcast to fields {lead}") from None
+    return np.ascontiguousarray(b).reshape(-1)
+
+
+def to_device(x, device, dtype=None) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        t = x.to(device)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(x)).to(device)
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.contiguous()
+
+
+INF = math.inf

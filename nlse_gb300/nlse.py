@@ -1,0 +1,435 @@
+"""NLSE solver class: the drop-in for the reference's NLSE with backend="GPU".
+
+Mirrors Quantum-Optics-LKB/NLSE v2.3.0, NLSE/nlse.py:41-681: same
+constructor, attributes, helper methods and out_field semantics.  Device
+arrays are torch CUDA tensors; the FFT, the propagator multiply and the
+nonlinear operator run in libnlse_sm103 (no CuPy, VkFFT or cuFFT).
+"""
+
+from __future__ import annotations
+
+import time
+import warnings
+from typing import Any, Callable, Union
+
+import numpy as np
+import torch
+from scipy import special
+from scipy.constants import c, epsilon_0
+
+from . import engine
+from .engine import OperatorData, Plan
+
+__BACKEND__ = "GPU"
+
+
+def _gpu_available() -> bool:
+    return torch.cuda.is_available()
+
+
+def _is_device_array(x) -> bool:
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _host(x):
+    """Host (NumPy) view of a parameter that may live on the device."""
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return x
+
+
+def count_steps(z: float, delta_z) -> int:
+    """Number of iterations of `while abs(z_prop) < z: z_prop += delta_z`.
+
+    Reproduces the float accumulation of the reference z-loop
+    (NLSE/nlse.py:568-585) exactly, so the step count matches it.
+    """
+    z_prop = 0
+    n = 0
+    if delta_z == 0:
+        if abs(z_prop) < z:
+            raise ValueError("delta_z = 0 with z > 0 never terminates")
+        return 0
+    while abs(z_prop) < z:
+        z_prop += delta_z
+        n += 1
+    return n
+
+
+class NLSE:
+    """A class to solve NLSE"""
+
+    __CUPY_AVAILABLE__ = _gpu_available()  # name kept from the reference: "GPU backend usable"
+    __GPU_AVAILABLE__ = __CUPY_AVAILABLE__
+    __PYOPENCL_AVAILABLE__ = False
+
+    _comps = 1  # field components stacked before the transform axes
+
+    def __init__(
+        self,
+        alpha: float,
+        power: float,
+        window: Union[float, tuple, list],
+        n2: float,
+        V: Union[np.ndarray, None],
+        L: float,
+        NX: int = 1024,
+        NY: int = 1024,
+        Isat: float = np.inf,
+        nl_length: float = 0,
+        wvl: float = 780e-9,
+        backend: str = __BACKEND__,
+    ) -> None:
+        """Instantiate the simulation (NLSE/nlse.py:47-155).
+
+        Solves d/dz psi = -1/2k0 (d2/dx2 + d2/dy2) psi + k0 dn psi + k0 n2 |psi|^2 psi.
+
+        Args:
+            alpha: linear loss (1/m); power: power in W; window: transverse window
+            in m (float or (wx, wy)); n2: nonlinear index (m^2/W); V: potential or
+            None; L: medium length (m); NX, NY: grid points; Isat: saturation
+            intensity (W/m^2); nl_length: nonlocal length (m); wvl: wavelength (m);
+            backend: "GPU" (the only backend of this engine).
+        """
+        self.backend = backend
+        self.n2 = n2
+        self.V = V
+        self.wl = wvl
+        self.k = 2 * np.pi / self.wl
+        self.L = L
+        self.alpha = alpha
+        self.power = power
+        self.I_sat = Isat
+        self.NX = NX
+        self.NY = NY
+        if isinstance(window, (float, int)):
+            self.window = [window, window]
+        elif isinstance(window, (tuple, list)):
+            self.window = window
+        else:
+            self.window = list(window)
+        # default step: 1/200 of the nonlinear length (nlse.py:108-114)
+        Dn = self.n2 * self.power / min(self.window) ** 2
+        z_nl = 1 / (self.k * abs(Dn))
+        if isinstance(z_nl, np.ndarray):
+            z_nl = float(z_nl.min())
+        self.delta_z = 5e-3 * z_nl
+        # float32 transverse grid, float64 step (nlse.py:116-131)
+        self.X, self.delta_X = np.linspace(
+            -self.window[0] / 2, self.window[0] / 2, num=NX, endpoint=False, retstep=True,
+            dtype=np.float32)
+        self.Y, self.delta_Y = np.linspace(
+            -self.window[1] / 2, self.window[1] / 2, num=NY, endpoint=False, retstep=True,
+            dtype=np.float32)
+        self._last_axes = (-2, -1)
+        self.XX, self.YY = np.meshgrid(self.X, self.Y)
+        self.Kx = 2 * np.pi * np.fft.fftfreq(self.NX, d=self.delta_X)
+        self.Ky = 2 * np.pi * np.fft.fftfreq(self.NY, d=self.delta_Y)
+        self.Kxx, self.Kyy = np.meshgrid(self.Kx, self.Ky)
+        self.propagator = None
+        self.plans = None
+        self.nl_length = nl_length
+        if self.nl_length > 0:
+            self.nl_profile = self._k0_profile(self.nl_length, self.delta_X)
+        else:
+            self.nl_profile = np.ones((self.NY, self.NX), dtype=np.float32)
+
+    @staticmethod
+    def _k0_profile(nl_length: float, delta_X: float) -> np.ndarray:
+        """Normalised K0 Bessel nonlocal kernel of size (6d+1)^2 (nlse.py:143-153)."""
+        d = nl_length // delta_X
+        r = np.arange(-3 * d, 3 * d + 1)
+        xx, yy = np.meshgrid(r, r)
+        prof = special.kn(0, np.hypot(xx, yy) / d)
+        finite = prof[np.logical_not(np.isinf(prof))]
+        prof[prof.shape[0] // 2, prof.shape[1] // 2] = np.nanmax(finite) if finite.size else np.nan
+        prof /= prof.sum()
+        return prof
+
+    # -- backend ------------------------------------------------------------
+    @property
+    def backend(self) -> str:
+        return self.__backend
+
+    @backend.setter
+    def backend(self, value: str) -> None:
+        """Select the backend (nlse.py:162-186).  This engine is the GPU backend."""
+        if value not in ["CPU", "GPU", "CL"]:
+            raise ValueError("Backend must be 'CPU', 'GPU' or 'CL'")
+        if value != "GPU":
+            raise ValueError(
+                f"backend {value!r} is not provided: this engine is the GPU backend only")
+        self.__backend = "GPU"
+
+    @property
+    def _device(self) -> torch.device:
+        return torch.device("cuda", torch.cuda.current_device())
+
+    # -- construction helpers (overridden by the subclasses) ------------------
+    def _build_propagator(self) -> np.ndarray:
+        """exp(-i (Kx^2+Ky^2)/(2k) dz) in FP64, cast to complex64 (nlse.py:188-197)."""
+        return np.exp(
+            -1j * 0.5 * (self.Kxx**2 + self.Kyy**2) / self.k * self.delta_z
+        ).astype(np.complex64)
+
+    def _build_fft_plan(self, A) -> list:
+        """One plan for both directions, as the reference's GPU path (nlse.py:199-218)."""
+        lead = self._lead_shape(tuple(A.shape))
+        n_axes = len(self._last_axes)
+        shape = tuple(A.shape[-n_axes:])
+        dtype = engine.dtype_code(A) if isinstance(A, torch.Tensor) else (
+            0 if np.dtype(A.dtype) == np.complex64 else 1)
+        nf = int(np.prod(lead)) if lead else 1
+        return [Plan.get(n_axes, shape, nf, self._comps, dtype, self._device)]
+
+    def _lead_shape(self, shape: tuple) -> tuple:
+        """Leading (batch) dimensions of a field shape."""
+        k = len(self._last_axes) + (1 if self._comps == 2 else 0)
+        return tuple(shape[: len(shape) - k])
+
+    def _norm_coef(self) -> float:
+        """Integration weight of sum(|E|^2) in the power normalisation (nlse.py:293-301)."""
+        return self.delta_X * self.delta_Y * c * epsilon_0 / 2
+
+    def _norm_target(self, lead: tuple) -> np.ndarray:
+        """Per-segment target of the normalisation (the power)."""
+        return engine.per_field(self.power, lead, 0, "power")
+
+    def _prepare_output_array(self, E_in, normalize: bool) -> tuple:
+        """Device copy of E_in, normalised to the power, and the |A|^2 twin (nlse.py:257-307)."""
+        dev = self._device
+        src = engine.to_device(E_in, dev)
+        A = torch.empty_like(src)
+        A_sq = torch.zeros(A.shape, dtype=A.real.dtype, device=dev)
+        if normalize:
+            lead = self._lead_shape(tuple(A.shape))
+            nseg = int(np.prod(lead)) * self._comps if lead else self._comps
+            sums = engine.power(src, nseg)
+            target = torch.from_numpy(np.ascontiguousarray(
+                self._norm_target(lead).reshape(-1))).to(dev)
+            engine.normalize(src, A, nseg, sums, target, self._norm_coef())
+        else:
+            A.copy_(src)
+        return A, A_sq
+
+    _DEVICE_ATTRS = ("power", "n2", "alpha", "I_sat")
+
+    def _send_arrays_to_gpu(self) -> None:
+        """Move the potential, propagator and array parameters to the device (nlse.py:309-342)."""
+        dev = self._device
+        if self.V is not None:
+            self.V = engine.to_device(self.V, dev)
+        self.nl_profile = engine.to_device(self.nl_profile, dev)
+        if self.propagator is not None:
+            self.propagator = engine.to_device(self.propagator, dev)
+        for name in self._DEVICE_ATTRS:
+            v = getattr(self, name, None)
+            if isinstance(v, np.ndarray):
+                setattr(self, name, engine.to_device(v, dev))
+
+    def _retrieve_arrays_from_gpu(self) -> None:
+        """Bring the device arrays back to NumPy (nlse.py:344-370)."""
+        if self.V is not None and _is_device_array(self.V):
+            self.V = self.V.cpu().numpy()
+        if _is_device_array(self.nl_profile):
+            self.nl_profile = self.nl_profile.cpu().numpy()
+        if _is_device_array(self.propagator):
+            self.propagator = self.propagator.cpu().numpy()
+        for name in self._DEVICE_ATTRS:
+            v = getattr(self, name, None)
+            if _is_device_array(v):
+                setattr(self, name, v.cpu().numpy())
+
+    # -- the split-step operator --------------------------------------------
+    def _nl_block(self, lead: tuple, precision: str, has_v: bool) -> np.ndarray:
+        """Per-field parameters of the nonlinear steps (nlse.py:404-487).
+
+        Row layout: see include/nlse_gb300.h (NLSE_PARAM_STRIDE).
+        """
+        nf = int(np.prod(lead)) if lead else 1
+        na = len(self._last_axes)
+        P = np.zeros((nf, 32), dtype=np.float64)
+        dz = self.delta_z
+        g = engine.per_field(self.k / 2 * _host(self.n2) * c * epsilon_0, lead, na, "n2")
+        alpha = engine.per_field(_host(self.alpha) / 2, lead, na, "alpha")
+        isat = engine.per_field(2 * _host(self.I_sat) / (epsilon_0 * c), lead, na, "Isat")
+        vs = self.k / 2
+        for s, dzs in ((0, dz / 2 if precision == "double" else dz), (1, dz / 2)):
+            o = s * 16
+            P[:, o + 0] = dzs
+            P[:, o + 1] = alpha
+            P[:, o + 2] = g
+            P[:, o + 3] = 0.0
+            P[:, o + 4] = isat
+            P[:, o + 5] = np.inf
+            P[:, o + 6] = vs
+        return P
+
+    def _prop_layout(self, prop: torch.Tensor) -> int:
+        """Element stride between the components' propagators (0: shared)."""
+        return 0
+
+    def _operator(self, A: torch.Tensor, V, propagator, precision: str,
+                  pump: tuple | None = None) -> OperatorData:
+        if precision not in ("single", "double"):
+            raise ValueError("precision must be 'single' or 'double'")
+        if self.nl_length > 0:
+            raise NotImplementedError("nonlocal response (nl_length > 0) is not available yet")
+        dev = A.device
+        lead = self._lead_shape(tuple(A.shape))
+        na = len(self._last_axes)
+        if isinstance(self.delta_z, complex):
+            raise NotImplementedError("imaginary-time evolution (complex delta_z)")
+        prop = engine.to_device(propagator, dev)
+        if prop.dtype not in (torch.complex64, torch.complex128):
+            prop = prop.to(torch.complex128 if A.dtype == torch.complex128 else torch.complex64)
+        Vd, vstride = None, 0
+        if V is not None:
+            Vd = engine.to_device(V, dev)
+            if Vd.is_complex() and not bool(torch.any(Vd.imag != 0)):
+                Vd = Vd.real.contiguous()
+            if A.dtype == torch.complex64:
+                Vd = Vd.to(torch.complex64 if Vd.is_complex() else torch.float32)
+            pix_shape = tuple(A.shape[-na:])
+            if tuple(Vd.shape[-na:]) != pix_shape:
+                raise ValueError(f"V of shape {tuple(Vd.shape)} does not match the grid {pix_shape}")
+            vlead = tuple(Vd.shape[:-na])
+            if vlead and int(np.prod(vlead)) > 1:
+                if vlead != lead:
+                    Vd = Vd.expand(*lead, *pix_shape).contiguous()
+                vstride = int(np.prod(pix_shape))
+            Vd = Vd.contiguous()
+        params = torch.from_numpy(self._nl_block(lead, precision, V is not None)).to(dev)
+        return OperatorData(prop=prop.contiguous(), params=params,
+                            scheme=1 if precision == "double" else 0,
+                            rabi=self._rabi_enabled(precision), V=Vd, v_fstride=vstride,
+                            prop_cstride=self._prop_layout(prop), pump=pump)
+
+    def _rabi_enabled(self, precision: str) -> bool:
+        return False
+
+    def split_step(
+        self,
+        A: torch.Tensor,
+        A_sq: torch.Tensor,
+        V,
+        propagator,
+        plans: list,
+        precision: str = "single",
+    ) -> None:
+        """One propagation step, in place on A (nlse.py:372-487).
+
+        A_sq is accepted for signature compatibility; |A|^2 is formed inside
+        the fused kernels and never stored.
+        """
+        op = self._operator(A, V, propagator, precision)
+        engine.propagate(plans[0], A, op, 1, 0, graph=False)
+
+    # -- pump hooks (DDGPE) ---------------------------------------------------
+    def _split_fused_callbacks(self, callback, callback_args, A):
+        """Separate callbacks the engine runs on the device from the host ones."""
+        return None, callback, callback_args
+
+    def out_field(
+        self,
+        E_in,
+        z: float,
+        plot: bool = False,
+        precision: str = "single",
+        verbose: bool = True,
+        normalize: bool = True,
+        callback: Union[list[Callable], Callable] = None,
+        callback_args: Union[list[tuple], tuple] = (),
+    ):
+        """Propagate the field over a distance z (nlse.py:489-619).
+
+        Without callbacks the whole z-loop is one nlse_propagate call replayed
+        from a CUDA graph; with callbacks each step is one call followed by the
+        callbacks on the live device field, as in the reference loop.
+        Returns the field in proper units (V/m): a NumPy array for NumPy input,
+        a torch tensor for torch input.
+        """
+        assert tuple(E_in.shape[self._last_axes[0]:]) == tuple(
+            self.XX.shape[self._last_axes[0]:]), "Shape mismatch"
+        in_dtype = E_in.dtype
+        assert in_dtype in (np.complex64, np.complex128, torch.complex64, torch.complex128), (
+            "Type mismatch, E_in should be complex64 or complex128")
+        if self.propagator is None:
+            self.propagator = self._build_propagator()
+        self._send_arrays_to_gpu()
+        V = None if self.V is None else self.V.clone()
+        A, A_sq = self._prepare_output_array(E_in, normalize)
+        self.plans = self._build_fft_plan(A)
+        if plot:
+            warnings.warn("plotting is not part of this engine; plot=True is ignored")
+        n2_old = self.n2
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+        t0 = time.perf_counter()
+        pump, callback, callback_args = self._split_fused_callbacks(callback, callback_args, A)
+        try:
+            if z > self.L:
+                self.n2 = 0
+            plen = None if pump is None else min(pump[1].numel(), pump[3].numel())
+            if callback is None:
+                n = count_steps(z, self.delta_z)
+                if plen is not None and n > plen:
+                    raise IndexError(f"the pump time profile has {plen} entries, the loop "
+                                     f"runs {n} steps")
+                if n > 0:
+                    op = self._operator(A, V, self.propagator, precision, pump)
+                    engine.propagate(self.plans[0], A, op, n, 0, graph=True)
+            else:
+                z_prop = 0
+                i = 0
+                op = None
+                key = None
+                while abs(z_prop) < z:
+                    if z > self.L:
+                        self.n2 = 0
+                    if plen is not None and i >= plen:
+                        raise IndexError(f"pump time profile index {i} out of range ({plen})")
+                    k = self._op_key()
+                    if op is None or k != key:
+                        op = self._operator(A, V, self.propagator, precision, pump)
+                        key = k
+                    engine.propagate(self.plans[0], A, op, 1, i, graph=False)
+                    if isinstance(callback, Callable):
+                        callback(self, A, z, i, *callback_args)
+                    elif isinstance(callback, list) and callback and isinstance(callback[0], Callable):
+                        for cb, ca in zip(callback, callback_args):
+                            cb(self, A, z, i, *ca)
+                    else:
+                        raise ValueError("callbacks should be a callable or a list of callables")
+                    z_prop += self.delta_z
+                    i += 1
+        finally:
+            self.n2 = n2_old
+        end.record()
+        if verbose:
+            end.synchronize()
+            print(f"\nTime spent to solve : {start.elapsed_time(end) * 1e-3} s (GPU) /"
+                  f" {time.perf_counter() - t0} s (CPU)\n")
+        self._retrieve_arrays_from_gpu()
+        if isinstance(E_in, np.ndarray):
+            return A.cpu().numpy()
+        if isinstance(E_in, torch.Tensor) and not E_in.is_cuda:
+            return A.cpu()
+        return A
+
+    def _op_key(self):
+        """Snapshot of the attributes the operator depends on (callbacks may change them)."""
+        def k(x):
+            if isinstance(x, torch.Tensor):
+                return ("t", x.data_ptr(), x._version)
+            if isinstance(x, np.ndarray):
+                return ("a", x.tobytes())
+            return x
+        return tuple(k(getattr(self, n, None)) for n in self._OP_ATTRS)
+
+    _OP_ATTRS = ("delta_z", "n2", "alpha", "I_sat", "k")
+
+    def plot_field(self, A_plot, z: float) -> None:
+        """Plotting is not provided (matplotlib is not a dependency of this engine)."""
+        raise NotImplementedError("plot_field is not part of this engine")

@@ -1,0 +1,177 @@
+"""Host-side logic of nlse_gb300 and the C ABI surface (no GPU needed)."""
+
+import ctypes as ct
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+from scipy.constants import c, epsilon_0
+
+import nlse_gb300 as ng
+from nlse_gb300 import _build, _lib, engine
+from oracle import nlse_oracle as orc
+from tests import cases
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "nlse_gb300.h"
+
+
+def _declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*|void)\s+(nlse_\w+)\(", text,
+                                 re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = _declared_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert {s for s, _, _ in _lib.SIGNATURES} == set(syms)
+
+
+def test_abi_version_and_error_reporting(lib):
+    assert lib.nlse_abi_version() == 1
+    h = ct.c_void_p()
+    d = _lib.Desc()
+    d.ndim = 2
+    d.shape[0], d.shape[1] = 100, 64  # not a power of two
+    d.nfields, d.comps, d.dtype = 1, 1, 0
+    rc = lib.nlse_plan_create(ct.byref(h), ct.byref(d))
+    assert rc == _lib.ERR_UNSUPPORTED
+    assert "powers of two" in _lib.last_error()
+    with pytest.raises(NotImplementedError):
+        _lib.check(rc)
+    d.ndim = 4
+    assert lib.nlse_plan_create(ct.byref(h), ct.byref(d)) == _lib.ERR_ARG
+    assert lib.nlse_power_workspace_size(3, 4096) == 3 * 8
+    assert lib.nlse_power(None, 0, 1, 1, None, None, 0, None) == _lib.ERR_ARG
+
+
+def test_backend_is_gpu_only():
+    with pytest.raises(ValueError):
+        ng.NLSE(20, 1.05, 1e-2, -1e-9, None, 1e-2, NX=8, NY=8, backend="CPU")
+    with pytest.raises(ValueError):
+        ng.NLSE(20, 1.05, 1e-2, -1e-9, None, 1e-2, NX=8, NY=8, backend="XYZ")
+
+
+@pytest.mark.parametrize("N", [64, 2048])
+def test_build_propagator_closed_forms(N):
+    """The reference's propagator KATs (tests/test_nlse.py:32-50 and per class)."""
+    s = ng.NLSE(cases.ALPHA, cases.POWER, cases.WINDOW, cases.N2, None, cases.L, NX=N, NY=N,
+                Isat=cases.ISAT)
+    p = s._build_propagator()
+    assert p.dtype == np.complex64
+    assert np.allclose(p, np.exp(-1j * 0.5 * (s.Kxx**2 + s.Kyy**2) / s.k * s.delta_z))
+    o = orc.OracleNLSE(cases.ALPHA, cases.POWER, cases.WINDOW, cases.N2, None, cases.L, NX=N,
+                       NY=N, Isat=cases.ISAT)
+    np.testing.assert_array_equal(p, o.build_propagator())
+    s1 = ng.NLSE_1d(cases.ALPHA, cases.POWER, cases.WINDOW, cases.N2, None, cases.L, NX=N)
+    p1 = s1._build_propagator()
+    assert p1.dtype == np.complex128
+    assert np.allclose(p1, np.exp(-1j * 0.5 * s1.Kx**2 / s1.k * s1.delta_z))
+    cn = ng.CNLSE(cases.ALPHA, cases.POWER, cases.WINDOW, cases.N2, -1e-10, None, cases.L,
+                  NX=N, NY=N)
+    cn.k2 = 2 * np.pi / 795e-9
+    pc = cn._build_propagator()
+    assert pc.shape == (2, N, N)
+    assert np.allclose(pc[1], np.exp(-1j * 0.5 * (cn.Kxx**2 + cn.Kyy**2) / cn.k2 * cn.delta_z))
+
+
+def test_nlse3d_and_gpe_and_ddgpe_propagators():
+    s = ng.NLSE_3d(alpha=20, energy=1.05 * 2e-6, window=np.array([8.92e-3, 16e-6]), n2=-1.6e-9,
+                   D0=1e-16, vg=3e7, V=None, L=1e-2, NX=16, NY=16, NZ=8, Isat=1e5)
+    p = s._build_propagator()
+    th = np.exp(-1j * 0.5 * (s.Kxx**2 + s.Kyy**2) / s.k * s.delta_z)
+    th = th * np.exp(-1j * s.D0 / 2 * s.Omega**2)
+    assert p.shape == (16, 16, 8) and p.dtype == np.complex128 and np.allclose(p, th)
+    from scipy.constants import hbar
+
+    g = ng.GPE(gamma=0, N=2e5, window=40e-6, g=1e-20, V=None, NX=32, NY=32)
+    g.delta_t = 1e-7
+    pg = g._build_propagator()
+    assert np.allclose(pg, np.exp(-1j * 0.5 * hbar * (g.Kxx**2 + g.Kyy**2) / g.m * 1e-7))
+    h = 0.654
+    d = ng.DDGPE(0.07 / h, 1.0, 64.0, 1e-2 / h, 5.07 / h, 2.0, 1484.44 / h, 1482.76 / h,
+                 0.17 / h, 27.0, NX=16, NY=16)
+    pd = d._build_propagator()
+    assert np.allclose(pd[0], np.exp(-1j * (d.omega_exc - d.omega_pump) * d.delta_z))
+
+
+def test_default_delta_z_and_grid_match_oracle():
+    for N in (32, 256):
+        s = ng.NLSE(20, 1.05, 8.92e-3, -1.6e-9, None, 1e-2, NX=N, NY=N)
+        o = orc.OracleNLSE(20, 1.05, 8.92e-3, -1.6e-9, None, 1e-2, NX=N, NY=N)
+        assert s.delta_z == o.delta_z
+        np.testing.assert_array_equal(s.XX, o.XX)
+        assert s.delta_X == o.delta_X
+
+
+def test_count_steps_matches_reference_loop():
+    assert ng.count_steps(10e-3, 5e-5) == 201
+    assert ng.count_steps(10e-3, 2e-5) == 501
+    assert ng.count_steps(20e-3, 5e-5) == 400
+    assert ng.count_steps(0, 5e-5) == 0
+    for z, dz in ((1e-3, 1e-5), (2e-3, 1e-4), (3.3e-3, 7e-5)):
+        assert ng.count_steps(z, dz) == orc.count_steps(z, dz)
+
+
+def test_per_field_broadcasting():
+    assert engine.per_field(2.0, (3,), 2, "x").tolist() == [2.0, 2.0, 2.0]
+    v = engine.per_field(np.arange(3.0).reshape(3, 1, 1), (3,), 2, "x")
+    assert v.tolist() == [0.0, 1.0, 2.0]
+    assert engine.per_field(np.arange(4.0), (4,), 0, "power").tolist() == [0, 1, 2, 3]
+    with pytest.raises(NotImplementedError):
+        engine.per_field(np.ones((3, 8, 8)), (3,), 2, "n2")  # varies over the grid
+    with pytest.raises(ValueError):
+        engine.per_field(np.ones((2, 1, 1)), (3,), 2, "n2")
+
+
+def test_nlse_parameter_block_formulas():
+    s = ng.NLSE(20, 1.05, 8.92e-3, -1.6e-9, None, 1e-2, NX=16, NY=16, Isat=1e5)
+    s.delta_z = 5e-5
+    P = s._nl_block((), "single", True)
+    assert P.shape == (1, 32)
+    assert P[0, 0] == 5e-5 and P[0, 1] == 10.0
+    assert P[0, 2] == s.k / 2 * s.n2 * c * epsilon_0
+    assert P[0, 4] == 2 * s.I_sat / (epsilon_0 * c) and np.isinf(P[0, 5])
+    assert P[0, 6] == s.k / 2
+    D = s._nl_block((), "double", True)
+    assert D[0, 0] == 2.5e-5 and D[0, 16] == 2.5e-5
+
+
+def test_ddgpe_parameter_block_follows_branch_arguments():
+    h = 0.654
+    d = ng.DDGPE(0.07 / h, 1.0, 64.0, 1e-2 / h, 5.07 / h, 2.0, 1484.44 / h, 1482.76 / h,
+                 0.17 / h, 27.0, NX=16, NY=16)
+    d.delta_z = 0.01
+    P = d._nl_block((), "single", False)
+    assert P[0, 1] == d.alpha / 2 and P[0, 8] == d.gamma2 / 2 and P[0, 9] == d.g2
+    assert P[0, 11] == d.I_sat and P[0, 12] == d.I_sat2
+    assert np.isclose(P[0, 14], np.cos(d.omega / 2 * 0.01)) and P[0, 30] == 0.01
+    D = d._nl_block((), "double", True)
+    assert D[0, 16] == 0.01 and D[0, 22] == 1.0  # before the linear step: full dz, raw V
+    assert D[0, 6] == d.k / 2 and D[0, 13] == 1.0  # after: k/2*V on the exciton only
+    D = d._nl_block((), "double", False)
+    assert D[0, 9] == d.g  # both components use g in this branch
+
+
+def test_cnlse_parameter_block():
+    cn = ng.CNLSE(20, 0.5, 8.92e-3, -1.6e-9, -0.8e-9, None, 2e-2, NX=16, NY=16, Isat=1e5,
+                  omega=2e3)
+    cn.n22 = -1.2e-9
+    cn.k2 = 2 * np.pi / 795e-9
+    P = cn._nl_block((), "single", False)
+    assert P[0, 3] == cn.k / 2 * cn.n12 * c * epsilon_0
+    assert P[0, 9] == cn.k2 / 2 * cn.n22 * c * epsilon_0
+    assert P[0, 10] == cn.k2 / 2 * cn.n12 * c * epsilon_0
+    assert P[0, 13] == cn.k2 / 2
+    assert np.isclose(P[0, 15], np.sin(1e3 * cn.delta_z))
+    assert cn._rabi_enabled("single") and not cn._rabi_enabled("double")
