@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Split-step throughput of nlse_gb300 on GB300, one JSON line on stdout.
+
+Workload: the NLSE 2-D beam at NX = NY = 2048, complex64, "single" scheme
+(power 1.05 W, waist 2.23 mm, window 4 waist, n2 = -1.6e-9 m^2/W,
+Isat = 1e5 W/m^2, alpha = 20 /m, potential -1e-4 exp(-r^2/(70 um)^2),
+E_0 (1 + 0.01 (a + ib)) with seeded normal a, b, dz = 2e-5 m).  A batch of
+8 such fields (256 MiB of complex64, more than the 129 MB L2) advances
+together, so every step streams from HBM; no L2 flush is needed.
+
+Metric: field-steps/s = fields x split steps / s (one split step of one
+2048^2 field is one "step").  `value` times nlse_propagate on resident
+device fields (the whole loop replayed from a CUDA graph); `e2e` times the
+public API, NLSE.out_field, from pinned host memory to host memory.
+
+--impl reference: the reference's CPU path restated by the oracle
+(reference CPU kernels: scipy FFT on all host cores + the numba kernels'
+arithmetic in NumPy), timed on one field per step.
+
+Multi-GPU (torchrun): every rank advances its own batch of fields (weak
+scaling, no collective on the data path); timing is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 2048
+BATCH = 8
+DZ = 2e-5
+WAIST, WAIST2, POWER, N2, ISAT, ALPHA, L = 2.23e-3, 70e-6, 1.05, -1.6e-9, 1e5, 20, 10e-3
+METRIC = "steps/s at 2048^2 c64 (field-steps/s, 8-field batch)"
+UNIT = "field-steps/s"
+# algorithmic bytes per grid point per step (complex64 field, real f32 potential)
+B_ROW = 16 + 4   # inverse+forward row pass: read A, write A, read V
+B_COL = 16       # column pass: read A, write A (propagator L2-resident, shared by the batch)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    return ap.parse_args()
+
+
+def fields(XX, YY, batch, seed):
+    rng = np.random.default_rng(seed)
+    E = np.exp(-(XX**2 + YY**2) / WAIST**2)
+    a = rng.standard_normal((batch, *XX.shape))
+    b = rng.standard_normal((batch, *XX.shape))
+    return (E * (1 + 0.01 * (a + 1j * b))).astype(np.complex64)
+
+
+def potential(XX, YY):
+    return (-1e-4 * np.exp(-(XX**2 + YY**2) / WAIST2**2)).astype(np.complex64)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read only)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic():
+    """DRAM bytes per launch of the column pass from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# reference CPU path (oracle restatement), bounded sample
+# ---------------------------------------------------------------------------
+def cpu_reference(steps_per_sample: int, reps: int, warmup: int):
+    from oracle import nlse_oracle as orc
+
+    cores = os.cpu_count() or 1
+    orc.WORKERS = cores
+    o = orc.OracleNLSE(ALPHA, POWER, 4 * WAIST, N2, None, L, NX=N, NY=N, Isat=ISAT,
+                       cpu_kernels=True)
+    o.delta_z = DZ
+    V = potential(o.XX, o.YY)
+    A = o.prepare(fields(o.XX, o.YY, 1, 0)[0], True)
+    prop = o.build_propagator()
+    for _ in range(warmup):
+        o.split_step(A, V, prop, "single")
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        for _ in range(steps_per_sample):
+            o.split_step(A, V, prop, "single")
+        times.append(time.perf_counter() - t0)
+    t = float(np.sum(times))
+    return {"value": reps * steps_per_sample / t, "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": f"{reps * steps_per_sample} split steps of one 2048^2 complex64 field, "
+                      "reference CPU-path arithmetic (kernels_cpu) with scipy.fft on all "
+                      "host threads"}, t
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cb, _ = cpu_reference(1, args.steps, max(0, min(args.warmup, 3)))
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / cb["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+            "config": {"workload": "NLSE 2-D 2048^2 complex64 single scheme, dz=2e-5 m, "
+                                   "potential well, noisy Gaussian beam; one field per step",
+                       "l2": "CPU run"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GB300 path
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+
+    import nlse_gb300 as ng
+    from nlse_gb300 import _build, _lib, engine
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    _build.build()
+    B = args.batch
+
+    sim = ng.NLSE(ALPHA, POWER, 4 * WAIST, N2, None, L, NX=N, NY=N, Isat=ISAT)
+    sim.delta_z = DZ
+    V = potential(sim.XX, sim.YY)
+    sim.V = V
+    E_host = fields(sim.XX, sim.YY, B, 1000 + rank)
+    A = torch.from_numpy(E_host).to(dev)
+    sim.propagator = sim._build_propagator()
+    plan = sim._build_fft_plan(A)[0]
+    op = sim._operator(A, torch.from_numpy(V).to(dev), sim.propagator, "single")
+
+    # warm-up (also captures and instantiates the graph)
+    engine.propagate(plan, A, op, args.warmup, 0, graph=True)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record()
+    engine.propagate(plan, A, op, args.steps, 0, graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    if dist:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * B * args.steps / t
+    launches = 1 + 2 * args.steps
+
+    # per-kernel durations on the launching stream (torch's current stream)
+    def time_pass(which, reps=20):
+        for _ in range(3):
+            engine.run_pass(plan, A, op, which)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            engine.run_pass(plan, A, op, which)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps / 1e3
+
+    t_col = time_pass(_lib.PASS_LINEAR)
+    t_row = time_pass(_lib.PASS_INV_NL_FWD)
+    npix = N * N * B
+    peak, peak_kind = peaks()
+    kern = {
+        "column_pass": {"s": t_col, "bytes": B_COL * npix},
+        "row_pass_inv_nl_fwd": {"s": t_row, "bytes": B_ROW * npix},
+    }
+    dom = max(kern, key=lambda k: kern[k]["s"])
+    ach = kern[dom]["bytes"] / kern[dom]["s"] / 1e9
+    traffic = load_traffic()
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak,
+            "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": round(ach / peak, 4),
+            "traffic": (traffic or {}).get(dom),
+            "algorithmic_bytes_per_launch": kern[dom]["bytes"],
+            "launch_ms": round(kern[dom]["s"] * 1e3, 4),
+            "other_kernels": {k: {"launch_ms": round(v["s"] * 1e3, 4),
+                                  "achieved_gbs": round(v["bytes"] / v["s"] / 1e9, 1)}
+                              for k, v in kern.items() if k != dom}}
+    step_model_gbs = 52 * N * N * B * args.steps / t / 1e9 / world
+
+    # e2e through the public API: pinned host field -> out_field -> host field
+    e2e = None
+    cpu_base = None
+    if True:
+        Eh = torch.from_numpy(E_host).pin_memory()
+        sim2 = ng.NLSE(ALPHA, POWER, 4 * WAIST, N2, None, L, NX=N, NY=N, Isat=ISAT)
+        sim2.delta_z = DZ
+        sim2.V = V
+        z = (args.steps - 0.5) * DZ
+        nst = ng.count_steps(z, DZ)
+        sim2.out_field(Eh, z, verbose=False)  # warm-up (plan, graph)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        out = sim2.out_field(Eh, z, verbose=False)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if dist:
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        h2d = E_host.nbytes + V.nbytes + sim2.propagator.nbytes
+        e2e = {"value": world * B * nst / te, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d / nst), "d2h_bytes_per_step": int(out.numpy().nbytes / nst),
+               "steps_per_call": nst, "note": "one out_field call from pinned host memory; "
+                                              "h2d/d2h bytes per call divided by its steps"}
+        # single 2048^2 field, the configuration's own 501-step loop (L2-resident)
+        s1 = ng.NLSE(ALPHA, POWER, 4 * WAIST, N2, None, L, NX=N, NY=N, Isat=ISAT)
+        s1.delta_z = DZ
+        s1.V = V
+        E1 = torch.from_numpy(E_host[0]).to(dev)
+        s1.out_field(E1, L, verbose=False)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)
+        ts = []
+        for _ in range(3):
+            flush.fill_(1)  # evict L2 between timed loops
+            a.record()
+            s1.out_field(E1, L, verbose=False)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        single = {"steps": ng.count_steps(L, DZ), "steps_per_s": ng.count_steps(L, DZ) / min(ts),
+                  "note": "one 2048^2 field, 501-step out_field loop from device memory, "
+                          "L2 flushed between loops (the field itself fits in L2)"}
+    if rank == 0:
+        cb, _ = cpu_reference(4, 3, 1)
+        cpu_base = cb
+        line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(t / args.steps * 1e3, 5), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+                "data": "synthetic (seeded noisy Gaussian beams)",
+                "config": {"workload": "NLSE 2-D 2048^2 complex64 single scheme, dz=2e-5 m, "
+                                       "potential well, noisy Gaussian beam (the 2048^2 "
+                                       "configuration), batch of fields per GPU",
+                           "fields_per_gpu": B, "grid": [N, N], "scheme": "single",
+                           "l2": "inputs larger than L2 (256 MiB per GPU)",
+                           "step_model_gbs_52B_per_pt": round(step_model_gbs, 1),
+                           "single_field_loop": single},
+                "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

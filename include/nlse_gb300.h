@@ -19,8 +19,8 @@
  *   ndim = 3: [nfields][NY][NX][NT]            (comps = 1)
  * The transform runs over the ndim trailing axes, batched over the rest, the
  * way the reference plans VkFFTApp(A.shape, ndim=len(_last_axes)) over the
- * trailing axes (NLSE/nlse.py:199-218).  Axis lengths are powers of two from
- * 2 to 4096.
+ * trailing axes (NLSE/nlse.py:199-218).  Transform axis lengths are powers
+ * of two from 2 to 4096.
  */
 #ifndef NLSE_GB300_H
 #define NLSE_GB300_H
@@ -87,6 +87,9 @@ typedef struct {
   const void* pump_t;    /* DDGPE pump time profile [steps] (field dtype) */
   const void* probe_r;   /* DDGPE probe spatial profile or NULL */
   const void* probe_t;
+  int64_t prop_version;  /* caller's version tag of the propagator contents: the plan keeps a
+                            re-laid-out copy of the propagator and refreshes it whenever the
+                            pointer, format or this tag changes */
 } nlse_operator;
 
 /* ABI version of the loaded library (NLSE_ABI_VERSION). */
@@ -97,8 +100,12 @@ const char* nlse_last_error(void);
 
 /*
  * Create a plan on the current CUDA device: validates the geometry, uploads
- * the twiddle table and sets the kernel attributes.  Replaces
- * NLSE._build_fft_plan (NLSE/nlse.py:199-218).
+ * the twiddle tables, allocates the plan's scratch (the blocked spectral
+ * buffer of 2-D plans, an FP32 copy of the parameter block) and sets the
+ * kernel attributes.  Replaces NLSE._build_fft_plan (NLSE/nlse.py:199-218).
+ * Axis lengths that are not powers of two from 2 to 4096 give a plan usable
+ * only by nlse_nonlinear; the transform entry points then return
+ * NLSE_ERR_UNSUPPORTED.
  */
 int nlse_plan_create(nlse_plan* out, const nlse_desc* desc);
 int nlse_plan_destroy(nlse_plan plan);
@@ -113,6 +120,28 @@ int nlse_plan_destroy(nlse_plan plan);
  */
 int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nsteps,
                    int64_t step0, int32_t flags, void* stream);
+
+/*
+ * One pass of the split-step sequence that nlse_propagate enqueues, so that
+ * a caller can time or compose the kernels one at a time:
+ *   NLSE_PASS_FORWARD     forward row pass (after the leading half nonlinear
+ *                         step of the "double" scheme)
+ *   NLSE_PASS_LINEAR      the strided-axis passes: forward column FFT,
+ *                         propagator multiply, inverse column FFT
+ *   NLSE_PASS_INV_NL_FWD  inverse row pass, 1/N, nonlinear step (step index
+ *                         `step` for the pump), next step's forward row pass
+ *   NLSE_PASS_INV_NL      inverse row pass, 1/N, nonlinear step
+ * A full step is FORWARD, LINEAR, INV_NL; n fused steps are FORWARD,
+ * (LINEAR, INV_NL_FWD) x (n-1), LINEAR, INV_NL.  Split of the loop body of
+ * NLSE.split_step (NLSE/nlse.py:372-487).  Not for 1-D plans (whose step is
+ * one pass: use nlse_propagate).
+ */
+#define NLSE_PASS_FORWARD 0
+#define NLSE_PASS_LINEAR 1
+#define NLSE_PASS_INV_NL_FWD 2
+#define NLSE_PASS_INV_NL 3
+int nlse_pass(nlse_plan plan, void* A, const nlse_operator* op, int32_t pass, int64_t step,
+              void* stream);
 
 /*
  * In-place transform over the plan's axes: forward (inverse = 0) or

@@ -16,6 +16,7 @@ NLSE_C64 = 0
 NLSE_C128 = 1
 NLSE_RUN_GRAPH = 1
 NLSE_PARAM_STRIDE = 32
+PASS_FORWARD, PASS_LINEAR, PASS_INV_NL_FWD, PASS_INV_NL = 0, 1, 2, 3
 
 OK = 0
 ERR_ARG = -1
@@ -50,6 +51,7 @@ class Operator(ct.Structure):
         ("pump_t", ct.c_void_p),
         ("probe_r", ct.c_void_p),
         ("probe_t", ct.c_void_p),
+        ("prop_version", ct.c_int64),
     ]
 
 
@@ -64,6 +66,11 @@ SIGNATURES = [
         ct.c_int,
         [ct.c_void_p, ct.c_void_p, ct.POINTER(Operator), ct.c_int64, ct.c_int64, ct.c_int32,
          ct.c_void_p],
+    ),
+    (
+        "nlse_pass",
+        ct.c_int,
+        [ct.c_void_p, ct.c_void_p, ct.POINTER(Operator), ct.c_int32, ct.c_int64, ct.c_void_p],
     ),
     ("nlse_fft", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
     (

@@ -37,8 +37,8 @@ int cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
 
-// Twiddle tables w[m] = exp(-2*pi*i*m/kNMax), one per device and precision,
-// computed in long double and rounded once.
+// Per-pass twiddle tables (fft_core.cuh), one array per device and
+// precision, computed in long double and rounded once.
 constexpr int kMaxDevices = 64;
 std::mutex g_tw_mu;
 void* g_tw[kMaxDevices][2] = {};
@@ -48,16 +48,20 @@ int get_twiddles(int dev, int dtype, const void** out) {
   std::lock_guard<std::mutex> lk(g_tw_mu);
   if (!g_tw[dev][dtype]) {
     const long double pi = 3.141592653589793238462643383279502884L;
-    std::vector<double> hd(2 * (size_t)kNMax);
-    for (int m = 0; m < kNMax; ++m) {
-      const long double ang = 2.0L * pi * (long double)m / (long double)kNMax;
-      hd[2 * m] = (double)cosl(ang);
-      hd[2 * m + 1] = (double)(-sinl(ang));
-    }
+    std::vector<double> hd(2 * (size_t)kTwTableLen);
+    for (int R = 2; R <= 16; R *= 2)
+      for (int NS = 1; NS * R <= kTwMaxLen; NS *= 2)
+        for (int r = 1; r < R; ++r)
+          for (int k = 0; k < NS; ++k) {
+            const size_t i = (size_t)tw_offset(R, NS) + (size_t)(r - 1) * NS + k;
+            const long double ang = 2.0L * pi * (long double)(r * k) / (long double)(NS * R);
+            hd[2 * i] = (double)cosl(ang);
+            hd[2 * i + 1] = (double)(-sinl(ang));
+          }
     void* d = nullptr;
     size_t bytes;
     if (dtype == NLSE_C64) {
-      std::vector<float> hf(2 * (size_t)kNMax);
+      std::vector<float> hf(2 * (size_t)kTwTableLen);
       for (size_t i = 0; i < hf.size(); ++i) hf[i] = (float)hd[i];
       bytes = hf.size() * sizeof(float);
       NLSE_CUDA(cudaMalloc(&d, bytes), "cudaMalloc(twiddles)");
@@ -102,6 +106,17 @@ struct nlse_plan_s {
   cudaGraphExec_t gexec = nullptr;
   GraphKey gkey;
   bool gvalid = false;
+  // 2-D fast path: spectral scratch in the blocked layout and the
+  // propagator converted to that layout (cached by pointer and format)
+  bool blk = false;
+  void* S = nullptr;
+  void* prop_blk = nullptr;
+  const void* prop_src = nullptr;
+  int prop_src_c128 = -1;
+  int64_t prop_src_cstride = -1;
+  int64_t prop_src_version = -1;
+  float* params_f32 = nullptr;  // FP32 mirror of the caller's parameter block
+  bool fft_ok = true;           // all axes are supported transform lengths
 };
 
 namespace {
@@ -119,6 +134,60 @@ cudaError_t cols(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a, cu
                  bool prep = false) {
   if (p->d.dtype == NLSE_C64) return launch_cols_f32(mode, log2n, a, s, prep);
   return launch_cols_f64(mode, log2n, a, s, prep);
+}
+
+cudaError_t cols_blk(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a, cudaStream_t s,
+                     bool prep = false) {
+  if (p->d.dtype == NLSE_C64) return launch_cols_blk_f32(mode, log2n, a, s, prep);
+  return launch_cols_blk_f64(mode, log2n, a, s, prep);
+}
+
+int blk_width(const nlse_plan_s* p) { return p->d.dtype == NLSE_C64 ? 4 : 2; }
+
+// Whether a 2-D plan can use the blocked spectral layout: the row pass needs
+// its threads-per-line (NX/16) and NX to be multiples of the block width,
+// the column pass at most 1024 threads (W * NY/16).
+bool blocked_ok(const nlse_desc& d) {
+  if (d.ndim != 2) return false;
+  const int64_t w = d.dtype == NLSE_C64 ? 4 : 2;
+  const int64_t nx = d.shape[1], ny = d.shape[0];
+  if (nx < 16 || ny < 16) return false;
+  if ((nx / 16) % w != 0) return false;
+  return w * (ny / 16) <= 1024;
+}
+
+// Column-pass arguments over the blocked spectral buffer.
+ColArgs col_blk_args(const nlse_plan_s* p, const nlse_operator* op) {
+  const nlse_desc& d = p->d;
+  ColArgs c{};
+  c.A = p->S;
+  c.tw = p->tw;
+  c.prop = p->prop_blk;
+  c.prop_cstride = op && op->prop_cstride ? p->pix : 0;
+  c.flags = (op && op->prop_c128) ? F_PROP_C128 : 0u;
+  c.comps = d.comps;
+  c.w = blk_width(p);
+  c.ld = c.w;
+  c.outer_stride = p->pix;
+  c.ncb = d.shape[1] / c.w;
+  c.nblocks = c.ncb * d.nfields * d.comps;
+  return c;
+}
+
+// Convert op->prop to the blocked layout unless the cached copy is current.
+int refresh_prop(nlse_plan_s* p, const nlse_operator* op, bool force, cudaStream_t s) {
+  if (!force && p->prop_src == op->prop && p->prop_src_c128 == op->prop_c128 &&
+      p->prop_src_cstride == op->prop_cstride && p->prop_src_version == op->prop_version)
+    return NLSE_OK;
+  const int64_t comps = op->prop_cstride ? p->d.comps : 1;
+  cudaError_t e = launch_prop_to_blk(op->prop_c128, op->prop, p->prop_blk, comps, p->d.shape[0],
+                                     p->d.shape[1], blk_width(p), s);
+  if (e != cudaSuccess) return cuda_fail(e, "propagator layout");
+  p->prop_src = op->prop;
+  p->prop_src_c128 = op->prop_c128;
+  p->prop_src_cstride = op->prop_cstride;
+  p->prop_src_version = op->prop_version;
+  return NLSE_OK;
 }
 
 // Columns per column-pass CTA: 64-byte row segments, bounded by the thread
@@ -158,7 +227,9 @@ StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
   const nlse_desc& d = p->d;
   StepArgs a{};
   a.A = A;
+  a.S = p->S;
   a.tw = p->tw;
+  a.params_f32 = p->params_f32;
   const int64_t n = d.shape[d.ndim - 1];
   a.lines_per_comp = p->pix / n;
   a.nq = d.nfields * a.lines_per_comp;
@@ -203,11 +274,89 @@ int check_op(const nlse_plan_s* p, const nlse_operator* op) {
   return NLSE_OK;
 }
 
+// One pass of the step sequence (see nlse_pass).
+int mirror_params(nlse_plan_s* p, const nlse_operator* op, cudaStream_t s) {
+  if (p->d.dtype != NLSE_C64) return NLSE_OK;
+  cudaError_t e = launch_params_f32(op->params, p->params_f32, p->d.nfields * kParamStride, s);
+  if (e != cudaSuccess) return cuda_fail(e, "parameter mirror");
+  return NLSE_OK;
+}
+
+int enqueue_pass(nlse_plan_s* p, void* A, const nlse_operator* op, int pass, int64_t step,
+                 cudaStream_t s) {
+  const nlse_desc& d = p->d;
+  if (d.ndim == 1) return fail(NLSE_ERR_UNSUPPORTED, "1-D plans have a single fused pass");
+  if (pass != NLSE_PASS_LINEAR) {
+    const int rc = mirror_params(p, op, s);
+    if (rc != NLSE_OK) return rc;
+  }
+  StepArgs a = row_args(p, A, op);
+  const uint32_t pre = op->scheme == 1 ? F_PRE_NL : 0u;
+  const int rl = p->lg[d.ndim - 1];
+  a.step = (int)step;
+  cudaError_t e = cudaSuccess;
+  if (p->blk) {
+    switch (pass) {
+      case NLSE_PASS_FORWARD:
+        a.flags |= pre | F_OUT_BLK;
+        e = rows(p, ROW_FWD, rl, a, s);
+        break;
+      case NLSE_PASS_LINEAR: {
+        const int rc = refresh_prop(p, op, false, s);
+        if (rc != NLSE_OK) return rc;
+        e = cols_blk(p, COL_FWD_PROP_INV, p->lg[0], col_blk_args(p, op), s);
+        break;
+      }
+      case NLSE_PASS_INV_NL_FWD:
+        a.flags |= pre | F_IN_BLK | F_OUT_BLK;
+        e = rows(p, ROW_INV_NL_FWD, rl, a, s);
+        break;
+      case NLSE_PASS_INV_NL:
+        a.flags |= F_IN_BLK;
+        e = rows(p, ROW_INV_NL, rl, a, s);
+        break;
+      default:
+        return fail(NLSE_ERR_ARG, "unknown pass %d", pass);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "pass");
+    return NLSE_OK;
+  }
+  switch (pass) {
+    case NLSE_PASS_FORWARD:
+      a.flags |= pre;
+      e = rows(p, ROW_FWD, rl, a, s);
+      break;
+    case NLSE_PASS_LINEAR:
+      if (d.ndim == 2) {
+        e = cols(p, COL_FWD_PROP_INV, p->lg[0], col_args(p, A, op, 0), s);
+      } else {
+        const ColArgs cx = col_args(p, A, op, 1);
+        e = cols(p, COL_FWD, p->lg[1], cx, s);
+        if (e == cudaSuccess) e = cols(p, COL_FWD_PROP_INV, p->lg[0], col_args(p, A, op, 0), s);
+        if (e == cudaSuccess) e = cols(p, COL_INV, p->lg[1], cx, s);
+      }
+      break;
+    case NLSE_PASS_INV_NL_FWD:
+      a.flags |= pre;
+      e = rows(p, ROW_INV_NL_FWD, rl, a, s);
+      break;
+    case NLSE_PASS_INV_NL:
+      e = rows(p, ROW_INV_NL, rl, a, s);
+      break;
+    default:
+      return fail(NLSE_ERR_ARG, "unknown pass %d", pass);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "pass");
+  return NLSE_OK;
+}
+
 // Enqueue nsteps split steps (no capture handling here).
 int enqueue_steps(nlse_plan_s* p, void* A, const nlse_operator* op, int64_t nsteps, int64_t step0,
                   cudaStream_t s) {
   const nlse_desc& d = p->d;
   if (nsteps <= 0) return NLSE_OK;
+  const int mrc = mirror_params(p, op, s);
+  if (mrc != NLSE_OK) return mrc;
   StepArgs a = row_args(p, A, op);
   const uint32_t pre = op->scheme == 1 ? F_PRE_NL : 0u;
   const int rl = p->lg[d.ndim - 1];
@@ -219,6 +368,32 @@ int enqueue_steps(nlse_plan_s* p, void* A, const nlse_operator* op, int64_t nste
     a.step = (int)step0;
     e = rows(p, ROW_FULL, rl, a, s);
     if (e != cudaSuccess) return cuda_fail(e, "row pass (1-D full step)");
+    return NLSE_OK;
+  }
+  if (p->blk) {
+    // A (natural) -> S (blocked): forward rows; S: columns; S -> S: inverse
+    // rows + nonlinear + next forward rows; S -> A: last inverse rows.
+    int rc = refresh_prop(p, op, false, s);
+    if (rc != NLSE_OK) return rc;
+    const ColArgs c = col_blk_args(p, op);
+    StepArgs a0 = a;
+    a0.flags |= pre | F_OUT_BLK;
+    e = rows(p, ROW_FWD, rl, a0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "row pass (forward)");
+    for (int64_t st = 0; st < nsteps; ++st) {
+      e = cols_blk(p, COL_FWD_PROP_INV, p->lg[0], c, s);
+      if (e != cudaSuccess) return cuda_fail(e, "column pass (linear step)");
+      StepArgs ai = a;
+      ai.step = (int)(step0 + st);
+      if (st + 1 < nsteps) {
+        ai.flags |= pre | F_IN_BLK | F_OUT_BLK;
+        e = rows(p, ROW_INV_NL_FWD, rl, ai, s);
+      } else {
+        ai.flags |= F_IN_BLK;
+        e = rows(p, ROW_INV_NL, rl, ai, s);
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "row pass (inverse + nonlinear)");
+    }
     return NLSE_OK;
   }
   // first forward row pass, with the step's leading half nonlinear step
@@ -264,6 +439,11 @@ int prepare_kernels(nlse_plan_s* p) {
       if (e != cudaSuccess) return cuda_fail(e, "kernel attributes (rows)");
     }
   }
+  if (p->blk) {
+    ColArgs c{};
+    cudaError_t e = cols_blk(p, COL_FWD_PROP_INV, p->lg[0], c, nullptr, true);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel attributes (blocked columns)");
+  }
   for (int ax = 0; ax + 1 < p->d.ndim; ++ax) {
     ColArgs c{};
     for (int m : {COL_FWD, COL_INV, COL_FWD_PROP_INV}) {
@@ -297,13 +477,12 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
   p->d = d;
   p->pix = 1;
   for (int k = 0; k < d.ndim; ++k) {
-    const int l = ilog2_pow2(d.shape[k]);
-    if (l < kMinLog2 || l > kMaxLog2) {
+    if (d.shape[k] < 1) {
       delete p;
-      return fail(NLSE_ERR_UNSUPPORTED,
-                  "axis %d has length %lld; this build transforms powers of two from 2 to %d", k,
-                  (long long)d.shape[k], 1 << kMaxLog2);
+      return fail(NLSE_ERR_ARG, "axis %d has length %lld", k, (long long)d.shape[k]);
     }
+    const int l = ilog2_pow2(d.shape[k]);
+    if (l < kMinLog2 || l > kMaxLog2) p->fft_ok = false;  // pointwise entry points only
     p->lg[k] = l;
     p->pix *= d.shape[k];
   }
@@ -313,13 +492,24 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     return cuda_fail(e, "cudaGetDevice");
   }
   int rc = get_twiddles(p->dev, d.dtype, &p->tw);
-  if (rc == NLSE_OK) rc = prepare_kernels(p);
+  p->blk = p->fft_ok && blocked_ok(d);
+  if (rc == NLSE_OK) {
+    e = cudaMalloc(&p->params_f32, (size_t)d.nfields * kParamStride * sizeof(float));
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(parameters)");
+  }
+  if (rc == NLSE_OK && p->blk) {
+    const size_t es = d.dtype == NLSE_C64 ? 8 : 16;
+    e = cudaMalloc(&p->S, (size_t)d.nfields * d.comps * p->pix * es);
+    if (e == cudaSuccess) e = cudaMalloc(&p->prop_blk, (size_t)d.comps * p->pix * 16);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(spectral scratch)");
+  }
+  if (rc == NLSE_OK && p->fft_ok) rc = prepare_kernels(p);
   if (rc == NLSE_OK) {
     e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
   }
   if (rc != NLSE_OK) {
-    delete p;
+    nlse_plan_destroy(p);
     return rc;
   }
   *out = p;
@@ -330,6 +520,9 @@ int nlse_plan_destroy(nlse_plan p) {
   if (!p) return NLSE_OK;
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   if (p->cap) cudaStreamDestroy(p->cap);
+  if (p->S) cudaFree(p->S);
+  if (p->prop_blk) cudaFree(p->prop_blk);
+  if (p->params_f32) cudaFree(p->params_f32);
   delete p;
   return NLSE_OK;
 }
@@ -339,6 +532,10 @@ int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps
   g_err.clear();
   if (!p || !A) return fail(NLSE_ERR_ARG, "null plan or field");
   if (nsteps < 0 || step0 < 0) return fail(NLSE_ERR_ARG, "negative step count or index");
+  if (!p->fft_ok)
+    return fail(NLSE_ERR_UNSUPPORTED,
+                "transform lengths must be powers of two from 2 to %d", 1 << kMaxLog2);
+
   int rc = check_op(p, op);
   if (rc != NLSE_OK) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -383,9 +580,27 @@ int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps
   return NLSE_OK;
 }
 
+int nlse_pass(nlse_plan p, void* A, const nlse_operator* op, int32_t pass, int64_t step,
+              void* stream) {
+  g_err.clear();
+  if (!p || !A) return fail(NLSE_ERR_ARG, "null plan or field");
+  if (step < 0) return fail(NLSE_ERR_ARG, "negative step index");
+  if (!p->fft_ok)
+    return fail(NLSE_ERR_UNSUPPORTED,
+                "transform lengths must be powers of two from 2 to %d", 1 << kMaxLog2);
+
+  int rc = check_op(p, op);
+  if (rc != NLSE_OK) return rc;
+  return enqueue_pass(p, A, op, pass, step, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int nlse_fft(nlse_plan p, void* A, int32_t inverse, void* stream) {
   g_err.clear();
   if (!p || !A) return fail(NLSE_ERR_ARG, "null plan or field");
+  if (!p->fft_ok)
+    return fail(NLSE_ERR_UNSUPPORTED,
+                "transform lengths must be powers of two from 2 to %d", 1 << kMaxLog2);
+
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const nlse_desc& d = p->d;
   // components are independent transforms here: view them as fields
@@ -415,6 +630,8 @@ int nlse_nonlinear(nlse_plan p, void* A, const void* asq, const nlse_operator* o
   if (!p || !A || !op || !op->params) return fail(NLSE_ERR_ARG, "null argument");
   if (p->d.dtype == NLSE_C64 && op->V && !op->v_f32)
     return fail(NLSE_ERR_ARG, "a complex64 field needs a single-precision potential");
+  const int mrc = mirror_params(p, op, reinterpret_cast<cudaStream_t>(stream));
+  if (mrc != NLSE_OK) return mrc;
   StepArgs a = row_args(p, A, op);
   a.asq = asq;
   if (asq) a.flags |= F_ASQ_EXT;

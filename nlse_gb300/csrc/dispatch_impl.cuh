@@ -66,8 +66,19 @@ static cudaError_t cols_n(const ColArgs& a, cudaStream_t s, bool prep) {
   constexpr int TPL = N / E;
   const int w = prep ? (kColMaxThreads / TPL > 0 ? kColMaxThreads / TPL : 1) : a.w;
   const size_t smem = size_t(padded_len(N)) * w * sizeof(cpx<T>);
-  auto kern = k_cols<T, N, E, MODE>;
-  if (prep) return set_smem(kern, smem);
+  // only the propagator pass has a complex128-propagator variant
+  constexpr bool HASP = MODE == COL_FWD_PROP_INV;
+  auto kern = k_cols<T, N, E, MODE, false>;
+  if constexpr (HASP) {
+    if (a.flags & F_PROP_C128) kern = k_cols<T, N, E, MODE, true>;
+  }
+  if (prep) {
+    if constexpr (HASP) {
+      cudaError_t e = set_smem(k_cols<T, N, E, MODE, true>, smem);
+      if (e != cudaSuccess) return e;
+    }
+    return set_smem(k_cols<T, N, E, MODE, false>, smem);
+  }
   if (w * TPL > kColMaxThreads) return cudaErrorInvalidConfiguration;
   if (a.nblocks <= 0) return cudaSuccess;
   kern<<<(unsigned)a.nblocks, w * TPL, smem, s>>>(a);
@@ -89,6 +100,48 @@ static cudaError_t cols_mode(int log2n, const ColArgs& a, cudaStream_t s, bool p
     case 10: return cols_n<T, 1024, MODE>(a, s, prep);
     case 11: return cols_n<T, 2048, MODE>(a, s, prep);
     case 12: return cols_n<T, 4096, MODE>(a, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T, int N, int MODE>
+static cudaError_t cols_blk_n(const ColArgs& a, cudaStream_t s, bool prep) {
+  constexpr int E = Shape<N>::E;
+  constexpr int THREADS = BlkW<T>::W * (N / E);
+  const size_t smem = size_t(padded_len(N)) * BlkW<T>::W * sizeof(cpx<T>);
+  auto kern = (a.flags & F_PROP_C128) ? k_cols_blk<T, N, E, MODE, true>
+                                      : k_cols_blk<T, N, E, MODE, false>;
+  if (prep) {
+    cudaError_t e = set_smem(k_cols_blk<T, N, E, MODE, true>, smem);
+    if (e != cudaSuccess) return e;
+    return set_smem(k_cols_blk<T, N, E, MODE, false>, smem);
+  }
+  if (a.nblocks <= 0) return cudaSuccess;
+  kern<<<(unsigned)a.nblocks, THREADS, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int MODE>
+static cudaError_t cols_blk_mode(int log2n, const ColArgs& a, cudaStream_t s, bool prep) {
+  switch (log2n) {
+    case 4: return cols_blk_n<T, 16, MODE>(a, s, prep);
+    case 5: return cols_blk_n<T, 32, MODE>(a, s, prep);
+    case 6: return cols_blk_n<T, 64, MODE>(a, s, prep);
+    case 7: return cols_blk_n<T, 128, MODE>(a, s, prep);
+    case 8: return cols_blk_n<T, 256, MODE>(a, s, prep);
+    case 9: return cols_blk_n<T, 512, MODE>(a, s, prep);
+    case 10: return cols_blk_n<T, 1024, MODE>(a, s, prep);
+    case 11: return cols_blk_n<T, 2048, MODE>(a, s, prep);
+    case 12: return cols_blk_n<T, 4096, MODE>(a, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+static cudaError_t cols_blk_dispatch(int mode, int log2n, const ColArgs& a, cudaStream_t s,
+                                     bool prep) {
+  switch (mode) {
+    case COL_FWD_PROP_INV: return cols_blk_mode<T, COL_FWD_PROP_INV>(log2n, a, s, prep);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -9,22 +9,37 @@
 // scattered to their Stockham positions in shared memory and gathered back
 // in the t + j*TPL pattern (P passes need P-1 exchanges).
 //
-// Radix order: radix-16 passes first, the remaining radix (2, 4 or 8) last,
+// Radix order: radix-min(16, E) passes first, the remaining radix last,
 // so that the small-stride scatter happens when the span NS is large.
 // Shared-memory index padding: one spare slot per 16 elements (padi), which
 // makes both the strided scatter of the first pass and the gathers
 // conflict-free for 8- and 16-byte elements.
 //
-// Twiddles come from one table w[m] = exp(-2*pi*i*m/NMAX) built on the host
-// in FP64 (rounded once to the element type), indexed with stride NMAX/N.
+// Twiddles: one table per (radix R, span NS) pass, laid out [r-1][k] with
+// entry exp(-2*pi*i*r*k/(NS*R)), r = 1..R-1, k = 0..NS-1, so that the lanes
+// of a warp (consecutive k) read consecutive entries.  All pass tables live
+// in one array built on the host in long double and rounded once to the
+// element type (tw_offset gives each pass's start).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace nlse {
 
-constexpr int kLog2NMax = 14;          // largest in-CTA line: 16384 points
-constexpr int kNMax = 1 << kLog2NMax;
+constexpr int kTwMaxLen = 4096;  // largest sub-transform NS*R covered by the tables
+
+// Start of the (R, NS) pass table: per radix R the tables for NS = 1, 2, 4, ...
+// follow each other ((R-1)*NS entries each), radices in the order 2, 4, 8, 16.
+__host__ __device__ constexpr int tw_radix_base(int R) {
+  return R == 2 ? 0
+       : R == 4 ? (kTwMaxLen - 1)
+       : R == 8 ? (kTwMaxLen - 1) + 3 * (kTwMaxLen / 2 - 1)
+                : (kTwMaxLen - 1) + 3 * (kTwMaxLen / 2 - 1) + 7 * (kTwMaxLen / 4 - 1);
+}
+__host__ __device__ constexpr int tw_offset(int R, int NS) {
+  return tw_radix_base(R) + (R - 1) * (NS - 1);
+}
+constexpr int kTwTableLen = tw_radix_base(16) + 15 * (kTwMaxLen / 8 - 1);
 
 template <typename T> struct CT;
 template <> struct CT<float> { using t = float2; };
@@ -163,20 +178,30 @@ template <int N, int EREQ = 16> struct Shape {
 // holds input position t + j*TPL; element j = s + r*BPT is input r of
 // butterfly b = t + s*TPL.  On exit x[s + r*BPT] holds output position
 // (b / NS) * NS * R + (b % NS) + r * NS.
+constexpr int TWG = 4;  // twiddles loaded per group
+
 template <typename T, int N, int E, int R, int NS, bool INV>
 __device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T>* __restrict__ tw) {
   constexpr int TPL = N / E, BPT = E / R;
-  constexpr int TWS = kNMax / N * (N / (NS * R));  // table stride per unit of r*k
+  static_assert(NS * R <= kTwMaxLen, "twiddle tables cover sub-transforms up to kTwMaxLen");
 #pragma unroll
   for (int s = 0; s < BPT; ++s) {
     cpx<T> y[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) y[r] = x[s + r * BPT];
     if constexpr (NS > 1) {
-      const int k = (t + s * TPL) & (NS - 1);
+      int k = (t + s * TPL) & (NS - 1);
+      // Opaque to the optimiser: without this the inverse transform's twiddle
+      // loads are merged with the forward ones and ~30 values stay live in
+      // registers across both transforms (register spills).
+      asm volatile("" : "+r"(k)::"memory");
+      const cpx<T>* twp = tw + tw_offset(R, NS) + k;
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        cpx<T> w = __ldg(&tw[(r * k) * TWS]);
+        // load and apply the twiddles in groups of TWG so that at most TWG
+        // of them are live at once (bounds register pressure)
+        if (r > 1 && (r - 1) % TWG == 0) asm volatile("" ::: "memory");
+        cpx<T> w = __ldg(twp + (r - 1) * NS);
         if (INV) w.y = -w.y;
         y[r] = cmul<T>(y[r], w);
       }
@@ -195,8 +220,15 @@ template <typename T, int N, int E, int NS, bool INV>
 __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
                                          const cpx<T>* __restrict__ tw) {
   constexpr int TPL = N / E;
-  constexpr int R = (N / NS) >= 16 ? 16 : (N / NS);
+  constexpr int RMAX = E < 16 ? E : 16;  // a butterfly never spans more than a thread's elements
+  constexpr int R = (N / NS) >= RMAX ? RMAX : (N / NS);
   constexpr int BPT = E / R;
+  static_assert(BPT >= 1 && BPT * R == E, "radix must divide the elements per thread");
+  if constexpr (NS == 1) {
+    // Recompute the shared-memory addresses in every transform instead of
+    // keeping those of an earlier transform in this kernel live in registers.
+    asm volatile("" : "+r"(t)::"memory");
+  }
   stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
   if constexpr (NS * R < N) {
     __syncthreads();

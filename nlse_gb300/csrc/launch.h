@@ -19,6 +19,9 @@ cudaError_t launch_rows_f64_c2(int mode, int log2n, const StepArgs& a, cudaStrea
 // Column passes (strided axis).
 cudaError_t launch_cols_f32(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
 cudaError_t launch_cols_f64(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
+// Column passes over the blocked spectral buffer (2-D fast path).
+cudaError_t launch_cols_blk_f32(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
+cudaError_t launch_cols_blk_f64(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
 
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction
@@ -28,5 +31,8 @@ cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int
                          const double* sums, const double* target, double coef, cudaStream_t s);
 cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStream_t s);
+cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t s);
+cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_t comps, int64_t ny,
+                               int64_t nx, int w, cudaStream_t s);
 
 }  // namespace nlse

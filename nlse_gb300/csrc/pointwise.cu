@@ -90,7 +90,7 @@ __global__ void k_nl_point(const StepArgs a) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = i / a.pix, px = i % a.pix;
-    const double* P = a.params + f * kParamStride;
+    const T* P = param_block<T>(a) + f * kParamStride;
     const int64_t i0 = (f * NC) * a.pix + px;
     const cpx<T> x0 = A[i0];
     T a0 = (a.flags & F_ASQ_EXT) ? asq[i0] : abs2<T>(x0);
@@ -108,14 +108,14 @@ __global__ void k_nl_point(const StepArgs a) {
       cpx<T> y0 = nl_point<T>(x0, a0, a1, p0, has_v, v0);
       cpx<T> y1 = nl_point<T>(x1, a1, a0, p1, has_v, v1);
       if (a.flags & F_RABI) {
-        const T rc = T(P[14]), rs = T(P[15]);
+        const T rc = P[14], rs = P[15];
         const cpx<T> z0 = mk<T>(rc * y0.x + rs * y1.y, rc * y0.y - rs * y1.x);
         const cpx<T> z1 = mk<T>(rc * y1.x + rs * y0.y, rc * y1.y - rs * y0.x);
         y0 = z0;
         y1 = z1;
       }
       if (a.flags & (F_PUMP | F_PROBE)) {
-        const T dz = T(P[30]);
+        const T dz = P[30];
         if (a.flags & F_PUMP) {
           cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[px],
                              reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]);
@@ -133,6 +133,12 @@ __global__ void k_nl_point(const StepArgs a) {
       A[i1] = y1;
     }
   }
+}
+
+__global__ void k_params_f32(const double* __restrict__ p, float* __restrict__ q, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = float(p[i]);
 }
 
 static unsigned grid_for(int64_t n, int threads) {
@@ -181,6 +187,25 @@ cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStre
   else
     k_abs2<double><<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(A),
                                                     reinterpret_cast<double*>(out), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_params_f32<<<grid_for(n, 256), 256, 0, s>>>(p, q, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_t comps, int64_t ny,
+                               int64_t nx, int w, cudaStream_t s) {
+  const int64_t total = comps * ny * nx;
+  if (total <= 0) return cudaSuccess;
+  if (prop_c128)
+    k_prop_to_blk<double><<<grid_for(total, 256), 256, 0, s>>>(
+        reinterpret_cast<const double2*>(nat), reinterpret_cast<double2*>(blk), total, ny, nx, w);
+  else
+    k_prop_to_blk<float><<<grid_for(total, 256), 256, 0, s>>>(
+        reinterpret_cast<const float2*>(nat), reinterpret_cast<float2*>(blk), total, ny, nx, w);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,8 @@
 // the cross terms set to g12 = 0, Isat2 = inf, |A2|^2 = 0, which adds exact
 // zeros.
 #pragma once
+#include <type_traits>
+
 #include "fft_core.cuh"
 
 namespace nlse {
@@ -39,10 +41,21 @@ enum : uint32_t {
   F_V_F32 = 1u << 9,      // potential stored in single precision: V' = vscale*V is
                           // formed in FP32 and then widened, as the reference does
                           // for a complex64 V with a complex128 field
+  F_IN_BLK = 1u << 10,    // row pass reads the blocked spectral buffer S
+  F_OUT_BLK = 1u << 11,   // row pass writes the blocked spectral buffer S
+};
+
+// Blocked spectral layout of a 2-D slab [NY][NX]: element (y, x) at
+// ((x / W) * NY + y) * W + x % W, W = 32 bytes / element size.  A column
+// tile (W columns x NY rows) is then one contiguous run, and a row is NX/W
+// runs of 32 bytes.
+template <typename T> struct BlkW {
+  static constexpr int W = 32 / int(sizeof(cpx<T>));
 };
 
 struct StepArgs {
-  void* A;                  // field, complex T, in place
+  void* A;                  // field, complex T, natural layout
+  void* S;                  // spectral scratch, blocked layout (2-D fast path), or null
   const void* V;            // potential: T or cpx<T>, null if absent
   const void* prop;         // propagator: cpx<float> or cpx<double>
   const double* params;     // [nfields][32]
@@ -51,7 +64,8 @@ struct StepArgs {
   const void* probe_r;
   const void* probe_t;
   const void* asq;          // T [nfields][comps][pixels] (nonlocal |A|^2), or null
-  const void* tw;           // twiddle table cpx<T> [kNMax]
+  const void* tw;           // per-pass twiddle tables cpx<T> [kTwTableLen]
+  const float* params_f32;  // FP32 mirror of params (complex64 kernels)
   int64_t nq;               // pixel-lines (fields * lines_per_comp)
   int64_t lines_per_comp;   // lines of one component of one field
   int64_t pix;              // pixels of one component of one field
@@ -79,19 +93,24 @@ struct ColArgs {
 };
 
 template <typename T> struct NLP {
-  T dz, alpha, gs, gc, is, ic;
-  double vs;
+  T dz, alpha, gs, gc, is, ic, vs;
 };
 
+// Parameters in the kernel's precision: complex64 kernels read the FP32
+// mirror of the block (rounded once per call by k_params_f32), so no FP64
+// instruction runs in their hot loops.
 template <typename T>
-__device__ __forceinline__ NLP<T> load_nlp(const double* __restrict__ p) {
+__device__ __forceinline__ const T* param_block(const StepArgs& a);
+
+template <typename T>
+__device__ __forceinline__ NLP<T> load_nlp(const T* __restrict__ p) {
   NLP<T> r;
-  r.dz = T(__ldg(p + 0));
-  r.alpha = T(__ldg(p + 1));
-  r.gs = T(__ldg(p + 2));
-  r.gc = T(__ldg(p + 3));
-  r.is = T(__ldg(p + 4));
-  r.ic = T(__ldg(p + 5));
+  r.dz = __ldg(p + 0);
+  r.alpha = __ldg(p + 1);
+  r.gs = __ldg(p + 2);
+  r.gc = __ldg(p + 3);
+  r.is = __ldg(p + 4);
+  r.ic = __ldg(p + 5);
   r.vs = __ldg(p + 6);
   return r;
 }
@@ -131,11 +150,22 @@ __device__ __forceinline__ T abs2(cpx<T> a) {
   return a.x * a.x + a.y * a.y;
 }
 
+template <>
+__device__ __forceinline__ const float* param_block<float>(const StepArgs& a) {
+  return a.params_f32;
+}
+template <>
+__device__ __forceinline__ const double* param_block<double>(const StepArgs& a) {
+  return a.params;
+}
+
 // V' = vscale * V rounded the way the reference rounds its k/2*V array: in
 // the storage precision of V, then widened to the field precision.
 template <typename T>
-__device__ __forceinline__ cpx<T> load_vp(const void* V, uint32_t flags, int64_t idx, double vs) {
-  if (flags & F_V_F32) {
+__device__ __forceinline__ cpx<T> load_vp(const void* V, uint32_t flags, int64_t idx, T vs) {
+  // complex64 fields always carry a single-precision potential (checked on
+  // the host); the FP64 branch must not even be if-converted into them
+  if (std::is_same<T, float>::value || (flags & F_V_F32)) {
     const float fs = float(vs);
     float2 v;
     if (flags & F_V_COMPLEX) v = __ldg(reinterpret_cast<const float2*>(V) + idx);
@@ -145,31 +175,27 @@ __device__ __forceinline__ cpx<T> load_vp(const void* V, uint32_t flags, int64_t
   double2 v;
   if (flags & F_V_COMPLEX) v = __ldg(reinterpret_cast<const double2*>(V) + idx);
   else v = make_double2(__ldg(reinterpret_cast<const double*>(V) + idx), 0.0);
-  return mk<T>(T(__dmul_rn(vs, v.x)), T(__dmul_rn(vs, v.y)));
+  return mk<T>(T(__dmul_rn(double(vs), v.x)), T(__dmul_rn(double(vs), v.y)));
 }
 
-template <typename T>
-__device__ __forceinline__ cpx<T> mul_prop(cpx<T> x, const void* prop, uint32_t flags, int64_t idx);
-
-template <>
-__device__ __forceinline__ float2 mul_prop<float>(float2 x, const void* prop, uint32_t flags,
-                                                  int64_t idx) {
-  if (flags & F_PROP_C128) {
-    // complex64 field times complex128 propagator: product in FP64, rounded
+// Field times propagator; PC128: the propagator is stored complex128 (a
+// compile-time choice: a runtime branch gets if-converted, putting FP64
+// multiplies, 1/64 of the FP32 rate on this part, into every complex64 step).
+template <typename T, bool PC128>
+__device__ __forceinline__ cpx<T> mul_prop(cpx<T> x, const void* prop, int64_t idx) {
+  if constexpr (PC128) {
     const double2 p = __ldg(reinterpret_cast<const double2*>(prop) + idx);
-    const double xr = x.x, xi = x.y;
-    return make_float2(float(xr * p.x - xi * p.y), float(xr * p.y + xi * p.x));
+    if constexpr (std::is_same<T, float>::value) {
+      // complex64 field times complex128 propagator: product in FP64, rounded
+      const double xr = x.x, xi = x.y;
+      return mk<T>(T(xr * p.x - xi * p.y), T(xr * p.y + xi * p.x));
+    } else {
+      return cmul<T>(x, mk<T>(T(p.x), T(p.y)));
+    }
+  } else {
+    const float2 p = __ldg(reinterpret_cast<const float2*>(prop) + idx);
+    return cmul<T>(x, mk<T>(T(p.x), T(p.y)));
   }
-  const float2 p = __ldg(reinterpret_cast<const float2*>(prop) + idx);
-  return cmul<float>(x, p);
-}
-
-template <>
-__device__ __forceinline__ double2 mul_prop<double>(double2 x, const void* prop, uint32_t flags,
-                                                    int64_t idx) {
-  if (flags & F_PROP_C128) return cmul<double>(x, __ldg(reinterpret_cast<const double2*>(prop) + idx));
-  const float2 p = __ldg(reinterpret_cast<const float2*>(prop) + idx);
-  return cmul<double>(x, make_double2(double(p.x), double(p.y)));
 }
 
 // Nonlinear step (set 0 or 1) for the E points a thread owns of one line.
@@ -179,7 +205,7 @@ __device__ __forceinline__ double2 mul_prop<double>(double2 x, const void* prop,
 template <typename T, int E, int TPL, int NC>
 __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], const StepArgs& a,
                                         int64_t f, int comp, int64_t pix0, int set, bool post) {
-  const double* P = a.params + f * kParamStride + set * 16;
+  const T* P = param_block<T>(a) + f * kParamStride + set * 16;
   const NLP<T> ps = load_nlp<T>(P + comp * 7);
   constexpr bool two = NC == 2;
   const bool rabi = two && post && (a.flags & F_RABI);
@@ -192,8 +218,8 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
   const int64_t qb_o = (f * NC + (1 - comp)) * a.pix + pix0;
   T rc = T(0), rs = T(0);
   if (rabi) {
-    rc = T(__ldg(a.params + f * kParamStride + 14));
-    rs = T(__ldg(a.params + f * kParamStride + 15));
+    rc = __ldg(param_block<T>(a) + f * kParamStride + 14);
+    rs = __ldg(param_block<T>(a) + f * kParamStride + 15);
   }
 #pragma unroll
   for (int j = 0; j < E; ++j) {
@@ -217,7 +243,7 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
   }
   if (two && post && comp == 1 && (a.flags & (F_PUMP | F_PROBE))) {
     // ddgpe.py:155-156: A2 -= F_r * F_t[i] * dz * 1j  (pump, then probe)
-    const T dz = T(__ldg(a.params + f * kParamStride + 30));
+    const T dz = __ldg(param_block<T>(a) + f * kParamStride + 30);
     const cpx<T>* pr = reinterpret_cast<const cpx<T>*>(a.pump_r);
     const cpx<T>* qr = reinterpret_cast<const cpx<T>*>(a.probe_r);
     const cpx<T> ptv = (a.flags & F_PUMP) ? reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]
@@ -282,14 +308,21 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
   const bool act = q < a.nq;
   const int64_t qq = act ? q : 0;
   const int64_t f = qq / a.lines_per_comp, m = qq % a.lines_per_comp;
-  C* A = reinterpret_cast<C*>(a.A) + ((f * nc + comp) * a.lines_per_comp + m) * (int64_t)N;
   const int64_t pix0 = m * N + t;
   C* sml = sm + lb * SL;
   constexpr bool two = NC == 2;
+  // source and destination: natural rows of A, or blocked rows of S
+  constexpr int W = BlkW<T>::W;
+  const int64_t slab = (f * nc + comp) * a.pix;
+  C* nat = reinterpret_cast<C*>(a.A) + slab + m * N + t;
+  C* blk = reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
+  const int64_t bstr = (int64_t)TPL * a.lines_per_comp;
+  const C* src = (a.flags & F_IN_BLK) ? blk : nat;
+  const int64_t sstr = (a.flags & F_IN_BLK) ? bstr : TPL;
 
   C x[E], xo[E];
 #pragma unroll
-  for (int j = 0; j < E; ++j) x[j] = act ? A[t + j * TPL] : mk<T>(T(0), T(0));
+  for (int j = 0; j < E; ++j) x[j] = act ? src[j * sstr] : mk<T>(T(0), T(0));
 
   if constexpr (MODE == ROW_FWD || MODE == ROW_FULL) {
     if (a.flags & F_PRE_NL) {
@@ -306,8 +339,13 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
       }
       fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
       const int64_t pb = comp * a.prop_cstride + t;
+      if (a.flags & F_PROP_C128) {
 #pragma unroll
-      for (int j = 0; j < E; ++j) x[j] = mul_prop<T>(x[j], a.prop, a.flags, pb + j * TPL);
+        for (int j = 0; j < E; ++j) x[j] = mul_prop<T, true>(x[j], a.prop, pb + j * TPL);
+      } else {
+#pragma unroll
+        for (int j = 0; j < E; ++j) x[j] = mul_prop<T, false>(x[j], a.prop, pb + j * TPL);
+      }
     }
     if constexpr (MODE == ROW_FWD) {
       fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
@@ -332,8 +370,10 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
     }
   }
   if (act) {
+    C* dst = (a.flags & F_OUT_BLK) ? blk : nat;
+    const int64_t dstr = (a.flags & F_OUT_BLK) ? bstr : TPL;
 #pragma unroll
-    for (int j = 0; j < E; ++j) A[t + j * TPL] = x[j];
+    for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
   }
 }
 
@@ -346,7 +386,7 @@ enum ColMode : int {
 
 constexpr int kColMaxThreads = 512;
 
-template <typename T, int N, int E, int MODE>
+template <typename T, int N, int E, int MODE, bool PC128>
 __global__ void __launch_bounds__(kColMaxThreads) k_cols(const ColArgs a) {
   using C = cpx<T>;
   constexpr int TPL = N / E;
@@ -366,11 +406,53 @@ __global__ void __launch_bounds__(kColMaxThreads) k_cols(const ColArgs a) {
     const int64_t pb = (o % a.comps) * a.prop_cstride + b * W + c;
 #pragma unroll
     for (int j = 0; j < E; ++j)
-      x[j] = mul_prop<T>(x[j], a.prop, a.flags, pb + (int64_t)(t + j * TPL) * a.ld);
+      x[j] = mul_prop<T, PC128>(x[j], a.prop, pb + (int64_t)(t + j * TPL) * a.ld);
     fft_line<T, N, E, 1, true>(x, t, sm + c, W, tw);
   }
 #pragma unroll
   for (int j = 0; j < E; ++j) base[(int64_t)(t + j * TPL) * a.ld] = x[j];
+}
+
+// Column pass over the blocked spectral buffer: CTA = one contiguous tile of
+// W columns x N rows (N = NY); a.A is S, a.prop the blocked propagator,
+// a.outer_stride the slab size NY*NX, a.ncb = NX / W.
+template <typename T, int N, int E, int MODE, bool PC128>
+__global__ void __launch_bounds__(BlkW<T>::W * (N / E)) k_cols_blk(const ColArgs a) {
+  using C = cpx<T>;
+  constexpr int TPL = N / E, W = BlkW<T>::W;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const int c = threadIdx.x % W, t = threadIdx.x / W;
+  const int64_t b = blockIdx.x % a.ncb, o = blockIdx.x / a.ncb;
+  const int64_t toff = b * (int64_t)(N * W) + t * W + c;
+  C* base = reinterpret_cast<C*>(a.A) + o * a.outer_stride + toff;
+  C x[E];
+#pragma unroll
+  for (int j = 0; j < E; ++j) x[j] = base[j * TPL * W];
+  fft_line<T, N, E, 1, MODE == COL_INV>(x, t, sm + c, W, tw);
+  if constexpr (MODE == COL_FWD_PROP_INV) {
+    const int64_t pb = (o % a.comps) * a.prop_cstride + toff;
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = mul_prop<T, PC128>(x[j], a.prop, pb + j * TPL * W);
+    fft_line<T, N, E, 1, true>(x, t, sm + c, W, tw);
+  }
+#pragma unroll
+  for (int j = 0; j < E; ++j) base[j * TPL * W] = x[j];
+}
+
+// Natural [comps][NY][NX] propagator -> blocked layout with block width W.
+template <typename TP>
+__global__ void k_prop_to_blk(const cpx<TP>* __restrict__ nat, cpx<TP>* __restrict__ blk,
+                              int64_t total, int64_t ny, int64_t nx, int w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pix = ny * nx;
+    const int64_t comp = i / pix, r = i % pix;
+    const int64_t bx = r / (ny * w), rem = r % (ny * w);
+    const int64_t y = rem / w, c = rem % w;
+    blk[i] = nat[comp * pix + y * nx + bx * w + c];
+  }
 }
 
 }  // namespace nlse

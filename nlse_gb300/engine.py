@@ -8,6 +8,7 @@ computes on the host beyond the small per-field parameter blocks.
 from __future__ import annotations
 
 import ctypes as ct
+import itertools
 import math
 from dataclasses import dataclass, field
 
@@ -17,6 +18,7 @@ import torch
 from . import _lib
 
 _DT = {torch.complex64: _lib.NLSE_C64, torch.complex128: _lib.NLSE_C128}
+_versions = itertools.count(1)
 
 
 def dtype_code(t: torch.Tensor) -> int:
@@ -110,6 +112,8 @@ class OperatorData:
     prop_cstride: int = 0
     pump: tuple | None = None  # (pump_r, pump_t, probe_r, probe_t) device tensors or None
     keep: list = field(default_factory=list)
+    # unique per operator: tells the plan its cached copy of the propagator is stale
+    version: int = field(default_factory=lambda: next(_versions))
 
     def struct(self) -> _lib.Operator:
         o = _lib.Operator()
@@ -130,6 +134,7 @@ class OperatorData:
                 o.pump_r, o.pump_t = pr.data_ptr(), pt.data_ptr()
             if qr is not None:
                 o.probe_r, o.probe_t = qr.data_ptr(), qt.data_ptr()
+        o.prop_version = int(self.version)
         return o
 
 
@@ -143,6 +148,15 @@ def propagate(plan: Plan, A: torch.Tensor, op: OperatorData, nsteps: int, step0:
         _lib.check(plan.lib.nlse_propagate(plan.handle, A.data_ptr(), ct.byref(s), int(nsteps),
                                            int(step0), flags, stream_handle(A.device)),
                    "propagate")
+
+
+def run_pass(plan: Plan, A: torch.Tensor, op: OperatorData, which: int, step: int = 0) -> None:
+    """Enqueue one pass of the step sequence (nlse_pass)."""
+    require_cuda(A)
+    s = op.struct()
+    with torch.cuda.device(A.device):
+        _lib.check(plan.lib.nlse_pass(plan.handle, A.data_ptr(), ct.byref(s), int(which),
+                                      int(step), stream_handle(A.device)), "pass")
 
 
 def nonlinear(plan: Plan, A: torch.Tensor, op: OperatorData, asq: torch.Tensor | None = None,
