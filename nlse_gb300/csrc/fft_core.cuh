@@ -236,12 +236,30 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
     for (int s = 0; s < BPT; ++s) {
       const int b = t + s * TPL;
       const int base = (b / NS) * NS * R + (b & (NS - 1));
+      // padi(base + r*NS) as one computed base plus compile-time offsets
+      // whenever the 16-element padding groups allow it
+      if constexpr (NS % 16 == 0) {
+        const int pb = padi(base) * stride;
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[padi(base + r * NS) * stride] = x[s + r * BPT];
+        for (int r = 0; r < R; ++r) sm[pb + r * (NS + NS / 16) * stride] = x[s + r * BPT];
+      } else if constexpr (NS == 1 && R == 16) {
+        const int pb = (17 * b) * stride;  // padi(16 b + r) = 17 b + r
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[pb + r * stride] = x[s + r * BPT];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[padi(base + r * NS) * stride] = x[s + r * BPT];
+      }
     }
     __syncthreads();
+    if constexpr (TPL % 16 == 0) {
+      const int pb = padi(t) * stride;  // padi(t + j TPL) = padi(t) + j (TPL + TPL/16)
 #pragma unroll
-    for (int j = 0; j < E; ++j) x[j] = sm[padi(t + j * TPL) * stride];
+      for (int j = 0; j < E; ++j) x[j] = sm[pb + j * (TPL + TPL / 16) * stride];
+    } else {
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = sm[padi(t + j * TPL) * stride];
+    }
     fft_line<T, N, E, NS * R, INV>(x, t, sm, stride, tw);
   }
 }

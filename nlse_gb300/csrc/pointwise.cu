@@ -98,7 +98,7 @@ __global__ void k_nl_point(const StepArgs a) {
     const int64_t vi = f * a.v_fstride + px;
     const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
     if constexpr (NC == 1) {
-      A[i0] = nl_point<T>(x0, a0, T(0), p0, has_v, v0);
+      A[i0] = nl_point<T, false>(x0, a0, T(0), p0, has_v, v0);
     } else {
       const int64_t i1 = i0 + a.pix;
       const cpx<T> x1 = A[i1];

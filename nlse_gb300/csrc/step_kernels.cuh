@@ -94,6 +94,7 @@ struct ColArgs {
 
 template <typename T> struct NLP {
   T dz, alpha, gs, gc, is, ic, vs;
+  T ris, ric;  // 1/is, 1/ic (per-thread reciprocals of the per-field constants)
 };
 
 // Parameters in the kernel's precision: complex64 kernels read the FP32
@@ -112,25 +113,94 @@ __device__ __forceinline__ NLP<T> load_nlp(const T* __restrict__ p) {
   r.is = __ldg(p + 4);
   r.ic = __ldg(p + 5);
   r.vs = __ldg(p + 6);
+  r.ris = T(1) / r.is;
+  r.ric = T(1) / r.ic;
   return r;
 }
 
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
-__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ float exp_t(float x) { return expf(x); }
-__device__ __forceinline__ double exp_t(double x) { return exp(x); }
+
+// ---- exp(re) * (cos(im), sin(im)) ------------------------------------------
+// The split step's per-step arguments are small (|re| = alpha*sat*dz,
+// |im| = phase per step), so the common case uses truncated Maclaurin series
+// of exp, sin and cos (Horner form), with enough terms that the truncation
+// error is far below one unit in the last place on the stated range:
+//   float:  |re| <= 1/16 (exp to x^7), |im| <= 1/2 (sin to x^11, cos to x^12)
+//   double: |re| <= 1/32 (exp to x^12), |im| <= 1/4 (sin to x^19, cos to x^20)
+// Outside the range the CUDA library functions are called from a non-inlined
+// helper, which keeps the unrolled kernels small.
+static __device__ __noinline__ void cis_exp_lib(float re, float im, float* cr, float* ci) {
+  float sn, cs;
+  sincosf(im, &sn, &cs);
+  const float e = expf(re);
+  *cr = e * cs;
+  *ci = e * sn;
+}
+static __device__ __noinline__ void cis_exp_lib(double re, double im, double* cr, double* ci) {
+  double sn, cs;
+  sincos(im, &sn, &cs);
+  const double e = exp(re);
+  *cr = e * cs;
+  *ci = e * sn;
+}
+
+template <typename T> struct CisRange;
+template <> struct CisRange<float> {
+  static constexpr float RE = 0.0625f, IM = 0.5f;
+  static constexpr int EXP_TERMS = 8, SIN_TERMS = 6, COS_TERMS = 7;
+};
+template <> struct CisRange<double> {
+  static constexpr double RE = 0.03125, IM = 0.25;
+  static constexpr int EXP_TERMS = 13, SIN_TERMS = 10, COS_TERMS = 11;
+};
+
+template <typename T>
+__device__ __forceinline__ void cis_exp(T re, T im, T* cr, T* ci) {
+  using R = CisRange<T>;
+  if (fabs(re) <= R::RE && fabs(im) <= R::IM) {
+    // exp(re) = 1 + re (1 + re/2 (1 + re/3 (...)))
+    // (the factors 1/k are compile-time constants; only the first two, 1 and
+    // 1/2, matter at the last bit and both are exact)
+    T e = T(1);
+#pragma unroll
+    for (int k = R::EXP_TERMS - 1; k >= 1; --k) e = fma(re * T(1.0 / k), e, T(1));
+    // sin(x) = x (1 - x^2/(2*3) (1 - x^2/(4*5) (...))), cos(x) = 1 - x^2/(1*2) (...)
+    const T x2 = im * im;
+    T sn = T(1), cs = T(1);
+#pragma unroll
+    for (int k = R::SIN_TERMS - 1; k >= 1; --k)
+      sn = fma(x2 * T(-1.0 / ((2 * k) * (2 * k + 1))), sn, T(1));
+    sn *= im;
+#pragma unroll
+    for (int k = R::COS_TERMS - 1; k >= 1; --k)
+      cs = fma(x2 * T(-1.0 / ((2 * k - 1) * (2 * k))), cs, T(1));
+    *cr = e * cs;
+    *ci = e * sn;
+  } else {
+    cis_exp_lib(re, im, cr, ci);
+  }
+}
 
 // One nonlinear sub-step on one point (kernels_gpu.py:68-104 form):
 //   sat = 1 / (1 + a_s/Isat_s + a_c/Isat_c)
 //   arg = i*(g_s*a_s*sat + g_c*a_c*sat) - alpha*sat + i*V',  V' = vscale*V
 //   A  *= exp(dz*arg)
-template <typename T>
+// TWO: the partner component's |A|^2 enters the saturation.  The divisions
+// a/Isat of the reference are multiplications by the per-field reciprocal
+// (within one rounding of the quotient); 1/(...) is the correctly rounded
+// reciprocal, identical to the reference's division of 1.
+template <typename T, bool TWO = true>
 __device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>& p, bool has_v,
                                            cpx<T> vp) {
-  const T sat = T(1) / (T(1) + a_s / p.is + a_c / p.ic);
-  T im = p.gs * a_s * sat + p.gc * a_c * sat;
+  T den = T(1) + a_s * p.ris;
+  if (TWO) den = den + a_c * p.ric;
+  const T sat = rcp_rn(den);
+  T im = p.gs * a_s * sat;
+  if (TWO) im = im + p.gc * a_c * sat;
   T re = -p.alpha * sat;
   if (has_v) {
     // arg += 1j * V'  ->  (re - Im V', im + Re V')
@@ -139,10 +209,9 @@ __device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>&
   }
   re = mul_rn(re, p.dz);
   im = mul_rn(im, p.dz);
-  const T e = exp_t(re);
-  T s, c;
-  sincos_t(im, &s, &c);
-  return cmul<T>(A, mk<T>(e * c, e * s));
+  T cr, ci;
+  cis_exp<T>(re, im, &cr, &ci);
+  return cmul<T>(A, mk<T>(cr, ci));
 }
 
 template <typename T>
@@ -202,9 +271,17 @@ __device__ __forceinline__ cpx<T> mul_prop(cpx<T> x, const void* prop, int64_t i
 // x: own component, xo: partner component (two-component models only, same
 // positions).  pix0: pixel index of position t within the component, the
 // thread's points are pix0 + j*TPL.
+// Real single-precision potential values of the thread's points, loaded at
+// kernel entry (before the FFT's barriers) so their latency is hidden.
+template <int E> struct VPre {
+  float v[E];
+  bool on;
+};
+
 template <typename T, int E, int TPL, int NC>
 __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], const StepArgs& a,
-                                        int64_t f, int comp, int64_t pix0, int set, bool post) {
+                                        int64_t f, int comp, int64_t pix0, int set, bool post,
+                                        const VPre<E>* vpre = nullptr) {
   const T* P = param_block<T>(a) + f * kParamStride + set * 16;
   const NLP<T> ps = load_nlp<T>(P + comp * 7);
   constexpr bool two = NC == 2;
@@ -231,12 +308,18 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
       as = abs2<T>(x[j]);
       if (two) ao = abs2<T>(xo[j]);
     }
-    const cpx<T> v = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, ps.vs) : mk<T>(T(0), T(0));
-    cpx<T> y = nl_point<T>(x[j], as, ao, ps, has_v, v);
+    cpx<T> v = mk<T>(T(0), T(0));
+    if (has_v) {
+      if (vpre && vpre->on)
+        v = mk<T>(T(__fmul_rn(float(ps.vs), vpre->v[j])), T(0));
+      else
+        v = load_vp<T>(a.V, a.flags, vb + j * TPL, ps.vs);
+    }
+    cpx<T> y = nl_point<T, two>(x[j], as, ao, ps, has_v, v);
     if (two && rabi) {
       // kernels_gpu.py:154-156: A1' = cos*A1 - i*sin*A2, A2' = cos*A2 - i*sin*A1
       const cpx<T> vo = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, po.vs) : mk<T>(T(0), T(0));
-      const cpx<T> yo = nl_point<T>(xo[j], ao, as, po, has_v, vo);
+      const cpx<T> yo = nl_point<T, two>(xo[j], ao, as, po, has_v, vo);
       y = mk<T>(rc * y.x + rs * yo.y, rc * y.y - rs * yo.x);
     }
     x[j] = y;
@@ -323,6 +406,14 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
   C x[E], xo[E];
 #pragma unroll
   for (int j = 0; j < E; ++j) x[j] = act ? src[j * sstr] : mk<T>(T(0), T(0));
+  VPre<E> vpre;
+  vpre.on = (MODE == ROW_INV_NL || MODE == ROW_INV_NL_FWD) && (a.flags & F_HAS_V) &&
+            (a.flags & F_V_F32) && !(a.flags & F_V_COMPLEX);
+  if (vpre.on) {
+    const float* vp = reinterpret_cast<const float*>(a.V) + f * a.v_fstride + pix0;
+#pragma unroll
+    for (int j = 0; j < E; ++j) vpre.v[j] = __ldg(vp + j * TPL);
+  }
 
   if constexpr (MODE == ROW_FWD || MODE == ROW_FULL) {
     if (a.flags & F_PRE_NL) {
@@ -357,7 +448,7 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
       if constexpr (MODE != ROW_INV) {
         if (!(a.flags & F_NO_POST)) {
           if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
-          nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true);
+          nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true, &vpre);
         }
       }
       if constexpr (MODE == ROW_INV_NL_FWD) {
