@@ -173,6 +173,28 @@ int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, doub
                void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * nlse_power without a workspace argument, for callers that cannot allocate
+ * device memory themselves -- for instance a plugin host whose device memory
+ * belongs to another framework's allocator, or code running between the
+ * launches of a replayed z-loop that must not allocate.  No counterpart in
+ * the reference.  The partial sums go to a static array inside the library
+ * (65,536 doubles, 512 KiB, held on every GPU that loads the library until
+ * the process exits), so:
+ *   - nseg * min(1024, ceil(seg_len / 8192)) must not exceed 65,536; larger
+ *     requests return NLSE_ERR_ARG with the numbers in nlse_last_error();
+ *   - the first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress), so make that first call before any stream
+ *     capture on that device;
+ *   - all calls share the array: calls whose kernels overlap on the GPU
+ *     (different streams without ordering between them) race and may
+ *     return wrong sums; order them on one stream.
+ * Nothing in the array needs clearing between calls: each call writes
+ * every partial it reads.  No device memory is allocated or freed.
+ */
+int nlse_power_noalloc(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, double* out,
+                       void* stream);
+
+/*
  * Power normalisation of _prepare_output_array (NLSE/nlse.py:284-307):
  * out[s] = in[s] * sqrt(target[s] / (sums[s] * coef)), the factor rounded to
  * the field precision.  in may equal out.

@@ -86,6 +86,11 @@ SIGNATURES = [
          ct.c_void_p],
     ),
     (
+        "nlse_power_noalloc",
+        ct.c_int,
+        [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p],
+    ),
+    (
         "nlse_normalize",
         ct.c_int,
         [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p,

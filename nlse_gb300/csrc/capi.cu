@@ -662,6 +662,26 @@ int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, doub
   return NLSE_OK;
 }
 
+int nlse_power_noalloc(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, double* out,
+                       void* stream) {
+  g_err.clear();
+  if (!A || !out) return fail(NLSE_ERR_ARG, "null argument");
+  if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
+  if (nseg < 0 || seg_len <= 0) return fail(NLSE_ERR_ARG, "bad segment geometry");
+  const int64_t need = nseg * (int64_t)power_chunks(seg_len);
+  if (need > noalloc_partials_max())
+    return fail(NLSE_ERR_ARG,
+                "nlse_power_noalloc: %lld segments of %lld elements need %lld partial sums, the "
+                "static array holds %lld (nseg * min(1024, ceil(seg_len / 8192)) must not exceed "
+                "it); use nlse_power with a workspace",
+                (long long)nseg, (long long)seg_len, (long long)need,
+                (long long)noalloc_partials_max());
+  cudaError_t e = launch_power_noalloc(dtype, A, nseg, seg_len, out,
+                                       reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "power (no allocation)");
+  return NLSE_OK;
+}
+
 int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64_t seg_len,
                    const double* sums, const double* target, double coef, void* stream) {
   g_err.clear();

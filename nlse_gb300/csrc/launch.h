@@ -25,6 +25,9 @@ cudaError_t launch_cols_blk_f64(int mode, int log2n, const ColArgs& a, cudaStrea
 
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction
+int64_t noalloc_partials_max();     // capacity of the static partial-sum array
+cudaError_t launch_power_noalloc(int dtype, const void* A, int64_t nseg, int64_t seg_len,
+                                 double* out, cudaStream_t s);
 cudaError_t launch_power(int dtype, const void* A, int64_t nseg, int64_t seg_len, double* partial,
                          int nchunks, double* out, cudaStream_t s);
 cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int64_t seg_len,

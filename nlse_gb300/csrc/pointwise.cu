@@ -1,5 +1,7 @@
 // Pointwise and reduction kernels: FP64 power sums, power normalisation,
 // the standalone nonlinear operator and |A|^2.
+#include <mutex>
+
 #include "launch.h"
 
 namespace nlse {
@@ -162,6 +164,41 @@ cudaError_t launch_power(int dtype, const void* A, int64_t nseg, int64_t seg_len
   if (e != cudaSuccess) return e;
   k_power_final<<<(unsigned)((nseg + 127) / 128), 128, 0, s>>>(partial, nchunks, nseg, out);
   return cudaGetLastError();
+}
+
+// ---- allocation-free power sums ---------------------------------------------
+// Partial sums of nlse_power_noalloc live in this file-scope device array
+// instead of a caller-provided workspace.  Every GPU that loads the library
+// holds it (512 KiB) until the process exits; all calls share it.
+constexpr int64_t kNoAllocPartials = 65536;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+int64_t noalloc_partials_max() { return kNoAllocPartials; }
+
+// Device address of the array on the current device, looked up once per
+// device (the name is only a host-side stand-in in host code).
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[64] = {};
+
+cudaError_t launch_power_noalloc(int dtype, const void* A, int64_t nseg, int64_t seg_len,
+                                 double* out, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  double* partial = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e != cudaSuccess) return e;
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    partial = g_noalloc_ptr[dev];
+  }
+  // every (segment, chunk) partial is written before it is read: nothing to clear
+  return launch_power(dtype, A, nseg, seg_len, partial, power_chunks(seg_len), out, s);
 }
 
 cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int64_t seg_len,
