@@ -41,7 +41,8 @@ typedef enum {
   NLSE_ERR_ARG = -1,         /* bad argument (null pointer, bad size, bad flag) */
   NLSE_ERR_UNSUPPORTED = -2, /* shape or option this build does not implement */
   NLSE_ERR_CUDA = -3,        /* a CUDA runtime call failed */
-  NLSE_ERR_STATE = -4        /* call not valid in the current state */
+  NLSE_ERR_STATE = -4,       /* call not valid in the current state */
+  NLSE_ERR_TIMEOUT = -5      /* a bounded wait inside a kernel gave up (see nlse_plan_status) */
 } nlse_status;
 
 /* nlse_propagate flags */
@@ -109,6 +110,14 @@ const char* nlse_last_error(void);
  */
 int nlse_plan_create(nlse_plan* out, const nlse_desc* desc);
 int nlse_plan_destroy(nlse_plan plan);
+
+/*
+ * Synchronise `stream` and report whether any kernel of this plan gave up a
+ * bounded wait since the last check (NLSE_ERR_TIMEOUT; the flag is then
+ * cleared).  Kernels that wait on asynchronous copies never spin without a
+ * deadline: on expiry they record the failure here and return.
+ */
+int nlse_plan_status(nlse_plan plan, void* stream);
 
 /*
  * Advance A in place by nsteps split steps of the reference's

@@ -23,6 +23,7 @@ ERR_ARG = -1
 ERR_UNSUPPORTED = -2
 ERR_CUDA = -3
 ERR_STATE = -4
+ERR_TIMEOUT = -5
 
 
 class Desc(ct.Structure):
@@ -61,6 +62,7 @@ SIGNATURES = [
     ("nlse_last_error", ct.c_char_p, []),
     ("nlse_plan_create", ct.c_int, [ct.POINTER(ct.c_void_p), ct.POINTER(Desc)]),
     ("nlse_plan_destroy", ct.c_int, [ct.c_void_p]),
+    ("nlse_plan_status", ct.c_int, [ct.c_void_p, ct.c_void_p]),
     (
         "nlse_propagate",
         ct.c_int,

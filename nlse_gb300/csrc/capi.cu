@@ -2,6 +2,7 @@
 // replay of the z-loop.  Declarations and contracts: include/nlse_gb300.h.
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -77,6 +78,37 @@ int get_twiddles(int dev, int dtype, const void** out) {
   return NLSE_OK;
 }
 
+// Tensor map of the blocked spectral buffer: dimensions (innermost first)
+// {2W scalars, NY, NX/W, nfields*comps}, one-row boxes of up to 256 runs.
+bool encode_tmap_S(CUtensorMap* tm, void* S, const nlse_desc& d, int64_t pix) {
+  using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                       &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return false;
+  const bool c64 = d.dtype == NLSE_C64;
+  const int64_t w = c64 ? 4 : 2;
+  const int64_t scalar = c64 ? 4 : 8;
+  const int64_t nb = d.shape[1] / w;
+  const cuuint64_t dims[4] = {(cuuint64_t)(2 * w), (cuuint64_t)d.shape[0], (cuuint64_t)nb,
+                              (cuuint64_t)(d.nfields * d.comps)};
+  const cuuint64_t strides[3] = {(cuuint64_t)(2 * w * scalar),
+                                 (cuuint64_t)(2 * w * scalar * d.shape[0]),
+                                 (cuuint64_t)(pix * 2 * scalar)};
+  const cuuint32_t box[4] = {(cuuint32_t)(2 * w), 1, (cuuint32_t)(nb < 256 ? nb : 256), 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = reinterpret_cast<EncodeFn>(fn)(
+      tm, c64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, S, dims,
+      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 int ilog2_pow2(int64_t n) {
   if (n < 2 || (n & (n - 1))) return -1;
   int l = 0;
@@ -117,6 +149,11 @@ struct nlse_plan_s {
   int64_t prop_src_version = -1;
   float* params_f32 = nullptr;  // FP32 mirror of the caller's parameter block
   bool fft_ok = true;           // all axes are supported transform lengths
+  int* status = nullptr;        // device status word: DEV_* codes from bounded waits
+  int nsm = 0;                  // multiprocessors (persistent grids)
+  bool cols_tma = true;         // use the TMA-ring column pass where it fits
+  bool rows_tma = false;        // tensor map of S encoded: TMA-fed inverse row passes
+  CUtensorMap tmS;              // S as {2W scalars, NY, NX/W, slabs}, box = one row (<= 256 runs)
 };
 
 namespace {
@@ -171,6 +208,8 @@ ColArgs col_blk_args(const nlse_plan_s* p, const nlse_operator* op) {
   c.outer_stride = p->pix;
   c.ncb = d.shape[1] / c.w;
   c.nblocks = c.ncb * d.nfields * d.comps;
+  c.status = p->status;
+  c.tma_grid = p->cols_tma ? p->nsm : 0;
   return c;
 }
 
@@ -230,6 +269,9 @@ StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
   a.S = p->S;
   a.tw = p->tw;
   a.params_f32 = p->params_f32;
+  a.status = p->status;
+  a.tma_grid = p->rows_tma ? p->nsm : 0;
+  a.tmap = p->rows_tma ? &p->tmS : nullptr;
   const int64_t n = d.shape[d.ndim - 1];
   a.lines_per_comp = p->pix / n;
   a.nq = d.nfields * a.lines_per_comp;
@@ -495,13 +537,23 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
   p->blk = p->fft_ok && blocked_ok(d);
   if (rc == NLSE_OK) {
     e = cudaMalloc(&p->params_f32, (size_t)d.nfields * kParamStride * sizeof(float));
-    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(parameters)");
+    if (e == cudaSuccess) e = cudaMalloc(&p->status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, p->dev);
+    if (e != cudaSuccess) rc = cuda_fail(e, "plan buffers");
+    const char* env = getenv("NLSE_COLS_TMA");
+    if (env && env[0] == '0') p->cols_tma = false;
   }
   if (rc == NLSE_OK && p->blk) {
     const size_t es = d.dtype == NLSE_C64 ? 8 : 16;
     e = cudaMalloc(&p->S, (size_t)d.nfields * d.comps * p->pix * es);
     if (e == cudaSuccess) e = cudaMalloc(&p->prop_blk, (size_t)d.comps * p->pix * 16);
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(spectral scratch)");
+    const char* env = getenv("NLSE_ROWS_TMA");
+    const bool want = !(env && env[0] == '0');
+    const int64_t nb = d.shape[1] / blk_width(p);
+    if (rc == NLSE_OK && want && (nb <= 256 || nb % 256 == 0) && d.nfields * d.comps < (1ll << 31))
+      p->rows_tma = encode_tmap_S(&p->tmS, p->S, d, p->pix);
   }
   if (rc == NLSE_OK && p->fft_ok) rc = prepare_kernels(p);
   if (rc == NLSE_OK) {
@@ -523,7 +575,24 @@ int nlse_plan_destroy(nlse_plan p) {
   if (p->S) cudaFree(p->S);
   if (p->prop_blk) cudaFree(p->prop_blk);
   if (p->params_f32) cudaFree(p->params_f32);
+  if (p->status) cudaFree(p->status);
   delete p;
+  return NLSE_OK;
+}
+
+int nlse_plan_status(nlse_plan p, void* stream) {
+  g_err.clear();
+  if (!p) return fail(NLSE_ERR_ARG, "null plan");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int h = 0;
+  NLSE_CUDA(cudaMemcpyAsync(&h, p->status, sizeof(int), cudaMemcpyDeviceToHost, s), "status read");
+  NLSE_CUDA(cudaStreamSynchronize(s), "status sync");
+  if (h != DEV_OK) {
+    NLSE_CUDA(cudaMemsetAsync(p->status, 0, sizeof(int), s), "status reset");
+    NLSE_CUDA(cudaStreamSynchronize(s), "status sync");
+    return fail(NLSE_ERR_TIMEOUT, "a bounded wait inside a kernel gave up (device code %d); the "
+                "results of the calls since the last status check are not valid", h);
+  }
   return NLSE_OK;
 }
 
@@ -652,6 +721,7 @@ int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, doub
   if (!A || !out) return fail(NLSE_ERR_ARG, "null argument");
   if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
   if (nseg < 0 || seg_len <= 0) return fail(NLSE_ERR_ARG, "bad segment geometry");
+  if (nseg > 65535) return fail(NLSE_ERR_UNSUPPORTED, "at most 65535 segments per call");
   const size_t need = nlse_power_workspace_size(nseg, seg_len);
   if (!workspace || workspace_bytes < need)
     return fail(NLSE_ERR_ARG, "workspace too small: %zu bytes needed", need);
@@ -668,6 +738,7 @@ int nlse_power_noalloc(const void* A, int32_t dtype, int64_t nseg, int64_t seg_l
   if (!A || !out) return fail(NLSE_ERR_ARG, "null argument");
   if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
   if (nseg < 0 || seg_len <= 0) return fail(NLSE_ERR_ARG, "bad segment geometry");
+  if (nseg > 65535) return fail(NLSE_ERR_UNSUPPORTED, "at most 65535 segments per call");
   const int64_t need = nseg * (int64_t)power_chunks(seg_len);
   if (need > noalloc_partials_max())
     return fail(NLSE_ERR_ARG,
@@ -687,6 +758,7 @@ int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64
   g_err.clear();
   if (!in || !out || !sums || !target) return fail(NLSE_ERR_ARG, "null argument");
   if (dtype != NLSE_C64 && dtype != NLSE_C128) return fail(NLSE_ERR_ARG, "dtype %d", dtype);
+  if (nseg > 65535) return fail(NLSE_ERR_UNSUPPORTED, "at most 65535 segments per call");
   cudaError_t e = launch_scale(dtype, in, out, nseg, seg_len, sums, target, coef,
                                reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "normalize");

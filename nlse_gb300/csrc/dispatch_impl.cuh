@@ -6,10 +6,43 @@
 
 namespace nlse {
 
+constexpr size_t kMaxSmemPerCta = 227 * 1024;
+
 template <typename F>
 static cudaError_t set_smem(F* kern, size_t smem) {
   if (smem <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// TMA-fed persistent variant of the inverse row passes on the blocked buffer.
+template <typename T, int N, int MODE, int NC>
+static cudaError_t rows_tma_n(const StepArgs& a, cudaStream_t s, bool prep, bool* used) {
+  *used = false;
+  constexpr bool OK_MODE = MODE == ROW_INV_NL || MODE == ROW_INV_NL_FWD;
+  constexpr int W = BlkW<T>::W;
+  if constexpr (OK_MODE && N >= 64 && (N / W) % ((N / W) < 256 ? (N / W) : 256) == 0 &&
+                rows_tma_smem<T, N, NC>() <= kMaxSmemPerCta) {
+    constexpr int E = Shape<N>::E;
+    constexpr int THREADS = NC * (N / E);
+    constexpr size_t smem = rows_tma_smem<T, N, NC>();
+    auto kern = k_rows_tma<T, N, E, MODE, NC>;
+    if (prep) {
+      *used = true;
+      return set_smem(kern, smem);
+    }
+    if (!(a.flags & F_IN_BLK) || a.tma_grid <= 0 || !a.tmap) return cudaSuccess;
+    *used = true;
+    if (a.nq <= 0) return cudaSuccess;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int64_t g = (int64_t)a.tma_grid * per_sm;
+    if (g > a.nq) g = a.nq;
+    kern<<<(unsigned)g, THREADS, smem, s>>>(a, *a.tmap);
+    return cudaGetLastError();
+  }
+  return cudaSuccess;
 }
 
 template <typename T, int N, int MODE, int NC>
@@ -18,6 +51,12 @@ static cudaError_t rows_n(const StepArgs& a, cudaStream_t s, bool prep) {
   using Cfg = RowCfg<N, E>;
   const size_t smem = size_t(Cfg::LPB) * Cfg::SL * sizeof(cpx<T>);
   auto kern = k_rows<T, N, E, MODE, NC>;
+  {
+    bool used = false;
+    cudaError_t e = rows_tma_n<T, N, MODE, NC>(a, s, prep, &used);
+    if (e != cudaSuccess) return e;
+    if (used && !prep) return cudaSuccess;
+  }
   if (prep) return set_smem(kern, smem);
   const int64_t per_block = Cfg::LPB / NC;
   const int64_t nblocks = (a.nq + per_block - 1) / per_block;
@@ -104,11 +143,43 @@ static cudaError_t cols_mode(int log2n, const ColArgs& a, cudaStream_t s, bool p
   }
 }
 
+// Persistent TMA-ring variant when two tiles and the exchange buffer fit in
+// shared memory (one CTA per SM, grid set by the plan).
+
+template <typename T, int N, int MODE>
+static cudaError_t cols_blk_tma_n(const ColArgs& a, cudaStream_t s, bool prep, int grid, bool* used) {
+  *used = false;
+  if constexpr (MODE == COL_FWD_PROP_INV && cols_tma_smem<T, N>() <= kMaxSmemPerCta && N >= 64) {
+    constexpr int E = Shape<N>::E;
+    constexpr int THREADS = BlkW<T>::W * (N / E);
+    constexpr size_t smem = cols_tma_smem<T, N>();
+    auto kern = (a.flags & F_PROP_C128) ? k_cols_blk_tma<T, N, E, true>
+                                        : k_cols_blk_tma<T, N, E, false>;
+    *used = true;
+    if (prep) {
+      cudaError_t e = set_smem(k_cols_blk_tma<T, N, E, true>, smem);
+      if (e != cudaSuccess) return e;
+      return set_smem(k_cols_blk_tma<T, N, E, false>, smem);
+    }
+    if (a.nblocks <= 0) return cudaSuccess;
+    const int64_t g = a.nblocks < grid ? a.nblocks : grid;
+    kern<<<(unsigned)g, THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+  }
+  return cudaSuccess;
+}
+
 template <typename T, int N, int MODE>
 static cudaError_t cols_blk_n(const ColArgs& a, cudaStream_t s, bool prep) {
   constexpr int E = Shape<N>::E;
   constexpr int THREADS = BlkW<T>::W * (N / E);
   const size_t smem = size_t(padded_len(N)) * BlkW<T>::W * sizeof(cpx<T>);
+  if (a.tma_grid > 0 || prep) {
+    bool used = false;
+    cudaError_t e = cols_blk_tma_n<T, N, MODE>(a, s, prep, a.tma_grid, &used);
+    if (e != cudaSuccess) return e;
+    if (used && !prep) return cudaSuccess;
+  }
   auto kern = (a.flags & F_PROP_C128) ? k_cols_blk<T, N, E, MODE, true>
                                       : k_cols_blk<T, N, E, MODE, false>;
   if (prep) {

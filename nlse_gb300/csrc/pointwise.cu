@@ -35,12 +35,14 @@ __global__ void __launch_bounds__(kRedThreads) k_power_partial(const cpx<T>* __r
   const int64_t lo = chunk * clen;
   const int64_t hi = lo + clen < seg_len ? lo + clen : seg_len;
   const cpx<T>* a = A + seg * seg_len;
-  double acc = 0.0;
+  // each thread sums its <= kRedChunk / kRedThreads points in the field
+  // precision (FP32 for complex64: <= 32 positive terms), then FP64 from here on
+  T tacc = T(0);
   for (int64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
     const cpx<T> v = a[i];
-    const double x = double(v.x), y = double(v.y);
-    acc += x * x + y * y;
+    tacc = fma(v.x, v.x, fma(v.y, v.y, tacc));
   }
+  double acc = double(tacc);
   __shared__ double ws[kRedThreads / 32];
   acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
@@ -61,16 +63,23 @@ __global__ void k_power_final(const double* __restrict__ partial, int nchunks, i
   out[seg] = s;
 }
 
+// grid (chunks, segments): the factor is computed once per block, in FP64,
+// and rounded to the field precision
 template <typename T>
 __global__ void k_scale(const cpx<T>* __restrict__ in, cpx<T>* __restrict__ out, int64_t seg_len,
-                        int64_t total, const double* __restrict__ sums,
-                        const double* __restrict__ target, double coef) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+                        const double* __restrict__ sums, const double* __restrict__ target,
+                        double coef) {
+  const int64_t seg = blockIdx.y;
+  __shared__ T sfac;
+  if (threadIdx.x == 0) sfac = T(sqrt(target[seg] / (sums[seg] * coef)));
+  __syncthreads();
+  const T s = sfac;
+  const cpx<T>* a = in + seg * seg_len;
+  cpx<T>* b = out + seg * seg_len;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < seg_len;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t seg = i / seg_len;
-    const T s = T(sqrt(target[seg] / (sums[seg] * coef)));
-    const cpx<T> v = in[i];
-    out[i] = mk<T>(v.x * s, v.y * s);
+    const cpx<T> v = a[i];
+    b[i] = mk<T>(v.x * s, v.y * s);
   }
 }
 
@@ -203,16 +212,17 @@ cudaError_t launch_power_noalloc(int dtype, const void* A, int64_t nseg, int64_t
 
 cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int64_t seg_len,
                          const double* sums, const double* target, double coef, cudaStream_t s) {
-  const int64_t total = nseg * seg_len;
-  if (total <= 0) return cudaSuccess;
+  if (nseg <= 0 || seg_len <= 0) return cudaSuccess;
+  int64_t gx = (seg_len + 256 * 8 - 1) / (256 * 8);
+  if (gx > 1024) gx = 1024;
+  const dim3 grid((unsigned)gx, (unsigned)nseg);
   if (dtype == 0)
-    k_scale<float><<<grid_for(total, 256), 256, 0, s>>>(reinterpret_cast<const float2*>(in),
-                                                        reinterpret_cast<float2*>(out), seg_len,
-                                                        total, sums, target, coef);
+    k_scale<float><<<grid, 256, 0, s>>>(reinterpret_cast<const float2*>(in),
+                                        reinterpret_cast<float2*>(out), seg_len, sums, target, coef);
   else
-    k_scale<double><<<grid_for(total, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(in),
-                                                         reinterpret_cast<double2*>(out), seg_len,
-                                                         total, sums, target, coef);
+    k_scale<double><<<grid, 256, 0, s>>>(reinterpret_cast<const double2*>(in),
+                                         reinterpret_cast<double2*>(out), seg_len, sums, target,
+                                         coef);
   return cudaGetLastError();
 }
 

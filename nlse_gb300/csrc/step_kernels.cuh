@@ -16,6 +16,7 @@
 #include <type_traits>
 
 #include "fft_core.cuh"
+#include "tma.cuh"
 
 namespace nlse {
 
@@ -76,10 +77,14 @@ struct StepArgs {
   int step;                 // step index (pump time profile)
   int nsteps;               // steps fused inside one launch (1-D full mode)
   uint32_t flags;
+  int* status;              // plan status word (bounded waits record timeouts here)
+  int tma_grid;             // >0: TMA-fed persistent inverse row pass with this many CTAs
+  const CUtensorMap* tmap;  // host pointer to the plan's tensor map of S (passed by value)
 };
 
 struct ColArgs {
   void* A;
+  int* status;              // plan status word (bounded waits record timeouts here)
   const void* prop;
   const void* tw;
   int64_t nblocks;          // column blocks * outer
@@ -90,6 +95,7 @@ struct ColArgs {
   int comps;                // outer index % comps selects the propagator component
   int w;                    // columns per block (power of two)
   uint32_t flags;
+  int tma_grid;             // >0: persistent TMA-ring column pass with this many CTAs
 };
 
 template <typename T> struct NLP {
@@ -468,6 +474,120 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
   }
 }
 
+// Persistent inverse row pass (ROW_INV_NL / ROW_INV_NL_FWD) on the blocked
+// spectral buffer, fed by tensor-map bulk copies: a blocked row is N/W runs
+// of W elements; the 4-D map {2W scalars, NY, N/W, slabs} with a box of one
+// row and up to 256 runs lands the row in shared memory in natural order.
+// Two stages: row q+grid is in flight while row q is transformed.
+constexpr int kRowStages = 2;
+
+template <typename T, int N, int NC>
+__host__ __device__ constexpr size_t rows_tma_smem() {
+  return (size_t)kRowStages * NC * N * sizeof(cpx<T>) +
+         (size_t)NC * padded_len(N) * sizeof(cpx<T>) + kRowStages * sizeof(uint64_t);
+}
+
+template <typename T, int N, int E, int MODE, int NC>
+__global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
+                                                          const __grid_constant__ CUtensorMap tmS) {
+  using C = cpx<T>;
+  constexpr int TPL = N / E, W = BlkW<T>::W, NB = N / W;
+  constexpr int BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
+  constexpr unsigned ROW_BYTES = N * sizeof(C);
+  constexpr int SL = padded_len(N);
+  constexpr bool two = NC == 2;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* stage = reinterpret_cast<C*>(smraw);
+  C* xch = stage + kRowStages * NC * N;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + NC * SL);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const int comp = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  const int64_t nq = a.nq;
+
+  auto issue = [&](int st, int64_t q) {
+    const int64_t f = q / a.lines_per_comp, y = q % a.lines_per_comp;
+    mbar_arrive_expect_tx(&bar[st], NC * ROW_BYTES);
+#pragma unroll
+    for (int cc = 0; cc < NC; ++cc)
+#pragma unroll
+      for (int bx = 0; bx < NBOX; ++bx)
+        tensor_load_4d(stage + (st * NC + cc) * N + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
+                       (int)(f * NC + cc), &bar[st]);
+  };
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kRowStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kRowStages; ++st) {
+      const int64_t q = blockIdx.x + (int64_t)st * gridDim.x;
+      if (q < nq) issue(st, q);
+    }
+  }
+  int it = 0;
+  for (int64_t q = blockIdx.x; q < nq; q += gridDim.x, ++it) {
+    const int st = it % kRowStages;
+    const unsigned par = (it / kRowStages) & 1;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+        if (q + gridDim.x < nq) mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kRowStages) & 1);
+      }
+      return;
+    }
+    const int64_t f = q / a.lines_per_comp, m = q % a.lines_per_comp;
+    const int64_t pix0 = m * N + t;
+    C x[E], xo[E];
+    const C* sp = stage + (st * NC + comp) * N + t;
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sp[j * TPL];
+    VPre<E> vpre;
+    vpre.on = (a.flags & F_HAS_V) && (a.flags & F_V_F32) && !(a.flags & F_V_COMPLEX);
+    if (vpre.on) {
+      const float* vp = reinterpret_cast<const float*>(a.V) + f * a.v_fstride + pix0;
+#pragma unroll
+      for (int j = 0; j < E; ++j) vpre.v[j] = __ldg(vp + j * TPL);
+    }
+    __syncthreads();  // every thread has read stage st
+    if (threadIdx.x == 0) {
+      const int64_t qn = q + (int64_t)kRowStages * gridDim.x;
+      if (qn < nq) {
+        fence_proxy_async_smem();
+        issue(st, qn);
+      }
+    }
+    C* xl = xch + comp * SL;
+    fft_line<T, N, E, 1, true>(x, t, xl, 1, tw);
+    const T sc = T(a.inv_n);
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], sc);
+    if (!(a.flags & F_NO_POST)) {
+      if (two) exchange_partner<T, N, E>(x, xo, xch, comp, t);
+      nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true, &vpre);
+    }
+    const int64_t slab = (f * NC + comp) * a.pix;
+    if constexpr (MODE == ROW_INV_NL_FWD) {
+      if (a.flags & F_PRE_NL) {
+        if (two) exchange_partner<T, N, E>(x, xo, xch, comp, t);
+        nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
+      }
+      fft_line<T, N, E, 1, false>(x, t, xl, 1, tw);
+      C* dst = reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
+      const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
+#pragma unroll
+      for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
+    } else {
+      C* dst = reinterpret_cast<C*>(a.A) + slab + m * N + t;
+#pragma unroll
+      for (int j = 0; j < E; ++j) dst[j * TPL] = x[j];
+    }
+  }
+}
+
 // ---- column kernels -------------------------------------------------------
 enum ColMode : int {
   COL_FWD = 0,
@@ -530,6 +650,99 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E)) k_cols_blk(const ColArgs
   }
 #pragma unroll
   for (int j = 0; j < E; ++j) base[j * TPL * W] = x[j];
+}
+
+// Persistent column pass over the blocked spectral buffer with a two-stage
+// bulk-copy ring: while a CTA transforms tile i from shared memory, the copy
+// engine brings tile i + gridDim.x into the other stage.  Results go straight
+// back to global memory (coalesced stores).  Same arithmetic as k_cols_blk.
+constexpr int kColStages = 2;
+
+template <typename T, int N>
+__host__ __device__ constexpr size_t cols_tma_smem() {
+  return (size_t)kColStages * N * BlkW<T>::W * sizeof(cpx<T>) +
+         (size_t)padded_len(N) * BlkW<T>::W * sizeof(cpx<T>) + kColStages * sizeof(uint64_t);
+}
+
+template <typename T, int N, int E, bool PC128>
+__global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const ColArgs a) {
+  using C = cpx<T>;
+  constexpr int TPL = N / E, W = BlkW<T>::W, TILE = N * W;
+  constexpr unsigned TILE_BYTES = TILE * sizeof(C);
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* stage = reinterpret_cast<C*>(smraw);
+  C* xch = stage + kColStages * TILE;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + padded_len(N) * W);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  C* S = reinterpret_cast<C*>(a.A);
+  const int c = threadIdx.x % W, t = threadIdx.x / W;
+  const int64_t ntiles = a.nblocks;
+  auto tile_ptr = [&](int64_t i) { return S + (i / a.ncb) * a.outer_stride + (i % a.ncb) * TILE; };
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kColStages; ++st) {
+      const int64_t i = blockIdx.x + (int64_t)st * gridDim.x;
+      if (i < ntiles) {
+        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+        bulk_load(stage + st * TILE, tile_ptr(i), TILE_BYTES, &bar[st]);
+      }
+    }
+  }
+  int it = 0;
+  for (int64_t i = blockIdx.x; i < ntiles; i += gridDim.x, ++it) {
+    const int st = it % kColStages;
+    const unsigned par = (it / kColStages) & 1;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      // give up: record it, let the copies in flight land (bounded), leave
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+        if (i + gridDim.x < ntiles)
+          mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kColStages) & 1);
+      }
+      return;
+    }
+    C x[E];
+    const C* sp = stage + st * TILE + t * W + c;
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sp[j * TPL * W];
+    const int64_t o = i / a.ncb;
+    const int64_t toff = (i % a.ncb) * (int64_t)TILE + t * W + c;
+    const int64_t pb = (o % a.comps) * a.prop_cstride + toff;
+    float2 pre[PC128 ? 1 : E];
+    if constexpr (!PC128) {
+      // propagator values (L2-resident) requested now, used after the forward FFT
+#pragma unroll
+      for (int j = 0; j < E; ++j) pre[j] = __ldg(reinterpret_cast<const float2*>(a.prop) + pb + j * TPL * W);
+    }
+    __syncthreads();  // every thread has read stage st
+    if (threadIdx.x == 0) {
+      const int64_t inext = i + (int64_t)kColStages * gridDim.x;
+      if (inext < ntiles) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+        bulk_load(stage + st * TILE, tile_ptr(inext), TILE_BYTES, &bar[st]);
+      }
+    }
+    fft_line<T, N, E, 1, false>(x, t, xch + c, W, tw);
+    if constexpr (PC128) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = mul_prop<T, true>(x[j], a.prop, pb + j * TPL * W);
+    } else {
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = cmul<T>(x[j], mk<T>(T(pre[j].x), T(pre[j].y)));
+    }
+    fft_line<T, N, E, 1, true>(x, t, xch + c, W, tw);
+    C* g = S + o * a.outer_stride + toff;
+#pragma unroll
+    for (int j = 0; j < E; ++j) g[j * TPL * W] = x[j];
+  }
 }
 
 // Natural [comps][NY][NX] propagator -> blocked layout with block width W.

@@ -79,6 +79,12 @@ class Plan:
             except Exception:
                 pass
 
+    def status(self) -> None:
+        """Synchronise and raise if a kernel of this plan gave up a bounded wait."""
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.nlse_plan_status(self.handle, stream_handle(self.device)),
+                       "plan status")
+
     # -- transforms -------------------------------------------------------
     def fft(self, A: torch.Tensor, B: torch.Tensor | None = None) -> torch.Tensor:
         """Forward transform over the plan axes (VkFFTApp.fft)."""
