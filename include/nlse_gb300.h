@@ -91,6 +91,9 @@ typedef struct {
   int64_t prop_version;  /* caller's version tag of the propagator contents: the plan keeps a
                             re-laid-out copy of the propagator and refreshes it whenever the
                             pointer, format or this tag changes */
+  const void* nl_khat;   /* nonlocal response: spectrum (field dtype) of the kernel placed on the
+                            plan's padded grid with its centre at the origin, or NULL for a local
+                            response; see nlse_plan_set_nonlocal */
 } nlse_operator;
 
 /* ABI version of the loaded library (NLSE_ABI_VERSION). */
@@ -129,6 +132,19 @@ int nlse_plan_status(nlse_plan plan, void* stream);
  */
 int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nsteps,
                    int64_t step0, int32_t flags, void* stream);
+
+/*
+ * Nonlocal response (the reference's oaconvolve(|A|^2, nl_profile, "same")
+ * over the transform axes, NLSE/nlse.py:143-155, 406-408, 444-447 and the
+ * CNLSE counterparts): give the plan a zero-padded grid pad_y x pad_x (1-D:
+ * pad_x only), powers of two at least N + M - 1 - (M-1)/2 per axis for a
+ * kernel of M points, so the cyclic convolution equals the linear "same" one.
+ * The plan allocates its padded scratch (nfields x pad_y x pad_x) here.
+ * pad_x = 0 removes it.  The operator then passes the kernel spectrum in
+ * nl_khat; each nonlinear step convolves |A|^2 (both components at once,
+ * as the real and imaginary parts) on the project FFT.
+ */
+int nlse_plan_set_nonlocal(nlse_plan plan, int64_t pad_y, int64_t pad_x);
 
 /*
  * One pass of the split-step sequence that nlse_propagate enqueues, so that

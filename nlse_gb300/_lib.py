@@ -53,6 +53,7 @@ class Operator(ct.Structure):
         ("probe_r", ct.c_void_p),
         ("probe_t", ct.c_void_p),
         ("prop_version", ct.c_int64),
+        ("nl_khat", ct.c_void_p),
     ]
 
 
@@ -63,6 +64,7 @@ SIGNATURES = [
     ("nlse_plan_create", ct.c_int, [ct.POINTER(ct.c_void_p), ct.POINTER(Desc)]),
     ("nlse_plan_destroy", ct.c_int, [ct.c_void_p]),
     ("nlse_plan_status", ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    ("nlse_plan_set_nonlocal", ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int64]),
     (
         "nlse_propagate",
         ct.c_int,

@@ -154,6 +154,10 @@ struct nlse_plan_s {
   bool cols_tma = true;         // use the TMA-ring column pass where it fits
   bool rows_tma = false;        // tensor map of S encoded: TMA-fed inverse row passes
   CUtensorMap tmS;              // S as {2W scalars, NY, NX/W, slabs}, box = one row (<= 256 runs)
+  // nonlocal response: zero-padded grid (py x px), its scratch and FFT plan
+  int64_t nl_py = 0, nl_px = 0;
+  void* X = nullptr;
+  nlse_plan_s* nlsub = nullptr;
 };
 
 namespace {
@@ -392,11 +396,86 @@ int enqueue_pass(nlse_plan_s* p, void* A, const nlse_operator* op, int pass, int
   return NLSE_OK;
 }
 
+int fft_sub(nlse_plan_s* q, void* X, int inverse, cudaStream_t s);
+
+// Nonlocal nonlinear step (parameter set `set`): pack |A|^2 into the padded
+// scratch, convolve by the kernel spectrum on the project FFT, apply the
+// pointwise step with the convolved intensities.
+int conv_nl(nlse_plan_s* p, void* A, const nlse_operator* op, int set, int64_t step,
+            cudaStream_t s) {
+  const nlse_desc& d = p->d;
+  const int64_t ny = d.ndim == 2 ? d.shape[0] : 1, nx = d.shape[d.ndim - 1];
+  const int64_t py = d.ndim == 2 ? p->nl_py : 1, px = p->nl_px;
+  cudaError_t e = launch_pack_asq(d.dtype, d.comps, A, p->X, d.nfields, ny, nx, py, px, s);
+  if (e != cudaSuccess) return cuda_fail(e, "nonlocal pack");
+  int rc = fft_sub(p->nlsub, p->X, 0, s);
+  if (rc != NLSE_OK) return rc;
+  e = launch_mul_spectrum(d.dtype, p->X, op->nl_khat, py * px, d.nfields * py * px, s);
+  if (e != cudaSuccess) return cuda_fail(e, "nonlocal spectrum");
+  rc = fft_sub(p->nlsub, p->X, 1, s);
+  if (rc != NLSE_OK) return rc;
+  StepArgs a = row_args(p, A, op);
+  a.step = (int)step;
+  if (set == 1) a.flags &= ~(F_RABI | F_PUMP | F_PROBE);
+  e = launch_nl_pointwise_pad(d.dtype, a, p->X, ny, nx, py, px, set, s);
+  if (e != cudaSuccess) return cuda_fail(e, "nonlocal nonlinear step");
+  return NLSE_OK;
+}
+
+// Split steps with the nonlocal response (no cross-step fusion: each
+// nonlinear step needs the convolution of the real-space intensity).
+int enqueue_steps_nonlocal(nlse_plan_s* p, void* A, const nlse_operator* op, int64_t nsteps,
+                           int64_t step0, cudaStream_t s) {
+  const nlse_desc& d = p->d;
+  if (!p->X) return fail(NLSE_ERR_STATE, "nonlocal kernel given but nlse_plan_set_nonlocal not called");
+  if (d.ndim == 3) return fail(NLSE_ERR_UNSUPPORTED, "nonlocal response of 3-D fields");
+  const int mrc = mirror_params(p, op, s);
+  if (mrc != NLSE_OK) return mrc;
+  const int rl = p->lg[d.ndim - 1];
+  cudaError_t e;
+  for (int64_t st = 0; st < nsteps; ++st) {
+    if (op->scheme == 1) {
+      const int rc = conv_nl(p, A, op, 1, step0 + st, s);
+      if (rc != NLSE_OK) return rc;
+    }
+    StepArgs a = row_args(p, A, op);
+    a.flags &= ~(F_PRE_NL);
+    if (d.ndim == 1) {
+      a.flags |= F_NO_POST;
+      a.nsteps = 1;
+      e = rows(p, ROW_FULL, rl, a, s);
+      if (e != cudaSuccess) return cuda_fail(e, "row pass (1-D linear step)");
+    } else if (p->blk) {
+      const int rc = refresh_prop(p, op, false, s);
+      if (rc != NLSE_OK) return rc;
+      StepArgs a0 = a;
+      a0.flags |= F_OUT_BLK;
+      e = rows(p, ROW_FWD, rl, a0, s);
+      if (e == cudaSuccess) e = cols_blk(p, COL_FWD_PROP_INV, p->lg[0], col_blk_args(p, op), s);
+      StepArgs a1 = a;
+      a1.flags |= F_IN_BLK | F_NO_POST;
+      if (e == cudaSuccess) e = rows(p, ROW_INV_NL, rl, a1, s);
+      if (e != cudaSuccess) return cuda_fail(e, "linear step");
+    } else {
+      e = rows(p, ROW_FWD, rl, a, s);
+      if (e == cudaSuccess) e = cols(p, COL_FWD_PROP_INV, p->lg[0], col_args(p, A, op, 0), s);
+      StepArgs a1 = a;
+      a1.flags |= F_NO_POST;
+      if (e == cudaSuccess) e = rows(p, ROW_INV_NL, rl, a1, s);
+      if (e != cudaSuccess) return cuda_fail(e, "linear step");
+    }
+    const int rc = conv_nl(p, A, op, 0, step0 + st, s);
+    if (rc != NLSE_OK) return rc;
+  }
+  return NLSE_OK;
+}
+
 // Enqueue nsteps split steps (no capture handling here).
 int enqueue_steps(nlse_plan_s* p, void* A, const nlse_operator* op, int64_t nsteps, int64_t step0,
                   cudaStream_t s) {
   const nlse_desc& d = p->d;
   if (nsteps <= 0) return NLSE_OK;
+  if (op->nl_khat) return enqueue_steps_nonlocal(p, A, op, nsteps, step0, s);
   const int mrc = mirror_params(p, op, s);
   if (mrc != NLSE_OK) return mrc;
   StepArgs a = row_args(p, A, op);
@@ -576,6 +655,8 @@ int nlse_plan_destroy(nlse_plan p) {
   if (p->prop_blk) cudaFree(p->prop_blk);
   if (p->params_f32) cudaFree(p->params_f32);
   if (p->status) cudaFree(p->status);
+  if (p->X) cudaFree(p->X);
+  if (p->nlsub) nlse_plan_destroy(p->nlsub);
   delete p;
   return NLSE_OK;
 }
@@ -661,6 +742,55 @@ int nlse_pass(nlse_plan p, void* A, const nlse_operator* op, int32_t pass, int64
   int rc = check_op(p, op);
   if (rc != NLSE_OK) return rc;
   return enqueue_pass(p, A, op, pass, step, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nlse_plan_set_nonlocal(nlse_plan p, int64_t pad_y, int64_t pad_x) {
+  g_err.clear();
+  if (!p) return fail(NLSE_ERR_ARG, "null plan");
+  const nlse_desc& d = p->d;
+  if (p->nlsub) {
+    nlse_plan_destroy(p->nlsub);
+    p->nlsub = nullptr;
+  }
+  if (p->X) {
+    cudaFree(p->X);
+    p->X = nullptr;
+  }
+  p->nl_py = p->nl_px = 0;
+  if (pad_x == 0) return NLSE_OK;
+  if (d.ndim == 3) return fail(NLSE_ERR_UNSUPPORTED, "nonlocal response of 3-D fields");
+  const int64_t nx = d.shape[d.ndim - 1], ny = d.ndim == 2 ? d.shape[0] : 1;
+  if (d.ndim == 1) pad_y = 1;
+  const int lx = ilog2_pow2(pad_x), ly = d.ndim == 2 ? ilog2_pow2(pad_y) : 1;
+  if (lx < kMinLog2 || lx > kMaxLog2 || ly < kMinLog2 || ly > kMaxLog2 || pad_x < nx ||
+      pad_y < ny)
+    return fail(NLSE_ERR_UNSUPPORTED,
+                "padded nonlocal grid %lld x %lld: powers of two from the grid size to %d",
+                (long long)pad_y, (long long)pad_x, 1 << kMaxLog2);
+  nlse_desc sd{};
+  sd.ndim = d.ndim;
+  if (d.ndim == 2) {
+    sd.shape[0] = pad_y;
+    sd.shape[1] = pad_x;
+  } else {
+    sd.shape[0] = pad_x;
+  }
+  sd.nfields = d.nfields;
+  sd.comps = 1;
+  sd.dtype = d.dtype;
+  nlse_plan q = nullptr;
+  int rc = nlse_plan_create(&q, &sd);
+  if (rc != NLSE_OK) return rc;
+  const size_t es = d.dtype == NLSE_C64 ? 8 : 16;
+  cudaError_t e = cudaMalloc(&p->X, (size_t)d.nfields * pad_y * pad_x * es);
+  if (e != cudaSuccess) {
+    nlse_plan_destroy(q);
+    return cuda_fail(e, "cudaMalloc(nonlocal scratch)");
+  }
+  p->nlsub = q;
+  p->nl_py = pad_y;
+  p->nl_px = pad_x;
+  return NLSE_OK;
 }
 
 int nlse_fft(nlse_plan p, void* A, int32_t inverse, void* stream) {
@@ -775,3 +905,10 @@ int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* st
 }
 
 }  // extern "C"
+
+namespace {
+// In-place transform of a plan's own geometry (used for the nonlocal scratch).
+int fft_sub(nlse_plan_s* q, void* X, int inverse, cudaStream_t s) {
+  return nlse_fft(q, X, inverse, s);
+}
+}  // namespace

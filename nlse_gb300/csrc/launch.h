@@ -35,6 +35,14 @@ cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int
 cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStream_t s);
 cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t s);
+// Nonlocal response: pack |A|^2 into the padded scratch, multiply by the
+// kernel spectrum, nonlinear step reading the convolved intensities.
+cudaError_t launch_pack_asq(int dtype, int nc, const void* A, void* X, int64_t nfields, int64_t ny,
+                            int64_t nx, int64_t py, int64_t px, cudaStream_t s);
+cudaError_t launch_mul_spectrum(int dtype, void* X, const void* K, int64_t per, int64_t total,
+                                cudaStream_t s);
+cudaError_t launch_nl_pointwise_pad(int dtype, const StepArgs& a, const void* X, int64_t ny,
+                                    int64_t nx, int64_t py, int64_t px, int set, cudaStream_t s);
 cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_t comps, int64_t ny,
                                int64_t nx, int w, cudaStream_t s);
 

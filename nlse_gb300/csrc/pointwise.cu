@@ -152,6 +152,90 @@ __global__ void k_params_f32(const double* __restrict__ p, float* __restrict__ q
     q[i] = float(p[i]);
 }
 
+// ---- nonlocal response ------------------------------------------------------
+// Pack |A|^2 of every field into the zero-padded complex scratch X
+// [nfields][py][px]: real part component 0, imaginary part component 1.
+template <typename T, int NC>
+__global__ void k_pack_asq(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ X, int64_t nfields,
+                           int64_t ny, int64_t nx, int64_t py, int64_t px) {
+  const int64_t per = py * px, total = nfields * per, pix = ny * nx;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / per, r = i % per, y = r / px, x = r % px;
+    cpx<T> v = mk<T>(T(0), T(0));
+    if (y < ny && x < nx) {
+      const int64_t a = (f * NC) * pix + y * nx + x;
+      v.x = abs2<T>(A[a]);
+      if (NC == 2) v.y = abs2<T>(A[a + pix]);
+    }
+    X[i] = v;
+  }
+}
+
+// X[slab][i] *= K[i] (kernel spectrum shared by the slabs).
+template <typename T>
+__global__ void k_mul_spectrum(cpx<T>* __restrict__ X, const cpx<T>* __restrict__ K, int64_t per,
+                               int64_t total) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    X[i] = cmul<T>(X[i], __ldg(K + i % per));
+}
+
+// Nonlinear step (parameter set 0) with |A|^2 taken from the convolved,
+// padded scratch X: component 0 from the real part, component 1 from the
+// imaginary part.
+template <typename T, int NC>
+__global__ void k_nl_point_pad(const StepArgs a, const cpx<T>* __restrict__ X, int64_t ny, int64_t nx,
+                               int64_t py, int64_t px, int set) {
+  const int64_t nf = a.nq / a.lines_per_comp;
+  const int64_t total = nf * a.pix;
+  cpx<T>* A = reinterpret_cast<cpx<T>*>(a.A);
+  const bool has_v = a.flags & F_HAS_V;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / a.pix, pxl = i % a.pix, y = pxl / nx, x = pxl % nx;
+    const cpx<T> c = X[(f * py + y) * px + x];
+    const T* P = param_block<T>(a) + f * kParamStride + set * 16;
+    const int64_t i0 = (f * NC) * a.pix + pxl;
+    const NLP<T> p0 = load_nlp<T>(P);
+    const int64_t vi = f * a.v_fstride + pxl;
+    const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
+    if constexpr (NC == 1) {
+      A[i0] = nl_point<T, false>(A[i0], c.x, T(0), p0, has_v, v0);
+    } else {
+      const int64_t i1 = i0 + a.pix;
+      const NLP<T> p1 = load_nlp<T>(P + 7);
+      const cpx<T> v1 = has_v ? load_vp<T>(a.V, a.flags, vi, p1.vs) : mk<T>(T(0), T(0));
+      cpx<T> y0 = nl_point<T>(A[i0], c.x, c.y, p0, has_v, v0);
+      cpx<T> y1 = nl_point<T>(A[i1], c.y, c.x, p1, has_v, v1);
+      if (a.flags & F_RABI) {
+        const T rc = P[14], rs = P[15];
+        const cpx<T> z0 = mk<T>(rc * y0.x + rs * y1.y, rc * y0.y - rs * y1.x);
+        const cpx<T> z1 = mk<T>(rc * y1.x + rs * y0.y, rc * y1.y - rs * y0.x);
+        y0 = z0;
+        y1 = z1;
+      }
+      if (a.flags & (F_PUMP | F_PROBE)) {
+        const T dz = P[30];
+        if (a.flags & F_PUMP) {
+          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[pxl],
+                             reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]);
+          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
+        }
+        if (a.flags & F_PROBE) {
+          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.probe_r)[pxl],
+                             reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]);
+          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
+        }
+      }
+      A[i0] = y0;
+      A[i1] = y1;
+    }
+  }
+}
+
 static unsigned grid_for(int64_t n, int threads) {
   int64_t g = (n + threads - 1) / threads;
   if (g > 152 * 32) g = 152 * 32;
@@ -253,6 +337,55 @@ cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_
   else
     k_prop_to_blk<float><<<grid_for(total, 256), 256, 0, s>>>(
         reinterpret_cast<const float2*>(nat), reinterpret_cast<float2*>(blk), total, ny, nx, w);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_asq(int dtype, int nc, const void* A, void* X, int64_t nfields, int64_t ny,
+                            int64_t nx, int64_t py, int64_t px, cudaStream_t s) {
+  const int64_t total = nfields * py * px;
+  if (total <= 0) return cudaSuccess;
+  const unsigned g = grid_for(total, 256);
+  if (dtype == 0) {
+    auto* a = reinterpret_cast<const float2*>(A);
+    auto* x = reinterpret_cast<float2*>(X);
+    if (nc == 1) k_pack_asq<float, 1><<<g, 256, 0, s>>>(a, x, nfields, ny, nx, py, px);
+    else k_pack_asq<float, 2><<<g, 256, 0, s>>>(a, x, nfields, ny, nx, py, px);
+  } else {
+    auto* a = reinterpret_cast<const double2*>(A);
+    auto* x = reinterpret_cast<double2*>(X);
+    if (nc == 1) k_pack_asq<double, 1><<<g, 256, 0, s>>>(a, x, nfields, ny, nx, py, px);
+    else k_pack_asq<double, 2><<<g, 256, 0, s>>>(a, x, nfields, ny, nx, py, px);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mul_spectrum(int dtype, void* X, const void* K, int64_t per, int64_t total,
+                                cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  const unsigned g = grid_for(total, 256);
+  if (dtype == 0)
+    k_mul_spectrum<float><<<g, 256, 0, s>>>(reinterpret_cast<float2*>(X),
+                                            reinterpret_cast<const float2*>(K), per, total);
+  else
+    k_mul_spectrum<double><<<g, 256, 0, s>>>(reinterpret_cast<double2*>(X),
+                                             reinterpret_cast<const double2*>(K), per, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nl_pointwise_pad(int dtype, const StepArgs& a, const void* X, int64_t ny,
+                                    int64_t nx, int64_t py, int64_t px, int set, cudaStream_t s) {
+  const int64_t total = (a.nq / a.lines_per_comp) * a.pix;
+  if (total <= 0) return cudaSuccess;
+  const unsigned g = grid_for(total, 256);
+  if (dtype == 0) {
+    auto* x = reinterpret_cast<const float2*>(X);
+    if (a.comps == 1) k_nl_point_pad<float, 1><<<g, 256, 0, s>>>(a, x, ny, nx, py, px, set);
+    else k_nl_point_pad<float, 2><<<g, 256, 0, s>>>(a, x, ny, nx, py, px, set);
+  } else {
+    auto* x = reinterpret_cast<const double2*>(X);
+    if (a.comps == 1) k_nl_point_pad<double, 1><<<g, 256, 0, s>>>(a, x, ny, nx, py, px, set);
+    else k_nl_point_pad<double, 2><<<g, 256, 0, s>>>(a, x, ny, nx, py, px, set);
+  }
   return cudaGetLastError();
 }
 

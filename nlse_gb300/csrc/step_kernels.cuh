@@ -504,8 +504,13 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   const int comp = threadIdx.x / TPL, t = threadIdx.x % TPL;
   const int64_t nq = a.nq;
 
+  // pixel-line q = (line y, field f) with the field fastest: CTAs of one wave
+  // take the same line of all fields and share its potential values in L2
+  const int64_t nf = nq / a.lines_per_comp;
+  auto q_f = [&](int64_t q) { return q % nf; };
+  auto q_y = [&](int64_t q) { return q / nf; };
   auto issue = [&](int st, int64_t q) {
-    const int64_t f = q / a.lines_per_comp, y = q % a.lines_per_comp;
+    const int64_t f = q_f(q), y = q_y(q);
     mbar_arrive_expect_tx(&bar[st], NC * ROW_BYTES);
 #pragma unroll
     for (int cc = 0; cc < NC; ++cc)
@@ -539,7 +544,7 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       }
       return;
     }
-    const int64_t f = q / a.lines_per_comp, m = q % a.lines_per_comp;
+    const int64_t f = q_f(q), m = q_y(q);
     const int64_t pix0 = m * N + t;
     C x[E], xo[E];
     const C* sp = stage + (st * NC + comp) * N + t;
@@ -677,7 +682,13 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
   C* S = reinterpret_cast<C*>(a.A);
   const int c = threadIdx.x % W, t = threadIdx.x / W;
   const int64_t ntiles = a.nblocks;
-  auto tile_ptr = [&](int64_t i) { return S + (i / a.ncb) * a.outer_stride + (i % a.ncb) * TILE; };
+  // tile i = (column block b, slab o) with the slab fastest: the CTAs of one
+  // wave transform the same column block of all fields, so each propagator
+  // tile is fetched from HBM once and then served from L2
+  const int64_t nouter = ntiles / a.ncb;
+  auto tile_o = [&](int64_t i) { return i % nouter; };
+  auto tile_b = [&](int64_t i) { return i / nouter; };
+  auto tile_ptr = [&](int64_t i) { return S + tile_o(i) * a.outer_stride + tile_b(i) * TILE; };
 
   if (threadIdx.x == 0) {
     for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
@@ -712,8 +723,8 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
     const C* sp = stage + st * TILE + t * W + c;
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sp[j * TPL * W];
-    const int64_t o = i / a.ncb;
-    const int64_t toff = (i % a.ncb) * (int64_t)TILE + t * W + c;
+    const int64_t o = tile_o(i);
+    const int64_t toff = tile_b(i) * (int64_t)TILE + t * W + c;
     const int64_t pb = (o % a.comps) * a.prop_cstride + toff;
     float2 pre[PC128 ? 1 : E];
     if constexpr (!PC128) {

@@ -79,6 +79,16 @@ class Plan:
             except Exception:
                 pass
 
+    def set_nonlocal(self, pads: tuple | None) -> None:
+        """Give the plan its zero-padded nonlocal grid (None removes it)."""
+        pads = tuple(int(x) for x in pads) if pads else None
+        if getattr(self, "_nl_pads", None) == pads:
+            return
+        py, px = (0, 0) if pads is None else ((1, pads[0]) if len(pads) == 1 else pads)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.nlse_plan_set_nonlocal(self.handle, py, px), "nonlocal grid")
+        self._nl_pads = pads
+
     def status(self) -> None:
         """Synchronise and raise if a kernel of this plan gave up a bounded wait."""
         with torch.cuda.device(self.device):
@@ -117,6 +127,7 @@ class OperatorData:
     v_fstride: int = 0
     prop_cstride: int = 0
     pump: tuple | None = None  # (pump_r, pump_t, probe_r, probe_t) device tensors or None
+    nl_khat: torch.Tensor | None = None  # nonlocal kernel spectrum on the padded grid
     keep: list = field(default_factory=list)
     # unique per operator: tells the plan its cached copy of the propagator is stale
     version: int = field(default_factory=lambda: next(_versions))
@@ -141,6 +152,8 @@ class OperatorData:
             if qr is not None:
                 o.probe_r, o.probe_t = qr.data_ptr(), qt.data_ptr()
         o.prop_version = int(self.version)
+        if self.nl_khat is not None:
+            o.nl_khat = self.nl_khat.data_ptr()
         return o
 
 
@@ -247,6 +260,37 @@ def per_field(x, lead: tuple, n_axes: int, name: str) -> np.ndarray:
     except ValueError:
         raise ValueError(f"{name} of shape {np.shape(x)} does not broadcast to fields {lead}") from None
     return np.ascontiguousarray(b).reshape(-1)
+
+
+def next_pow2(n: int) -> int:
+    p = 1
+    while p < n:
+        p *= 2
+    return p
+
+
+def nonlocal_spectrum(profile, grid: tuple, dtype: torch.dtype, device) -> tuple:
+    """Padded grid and kernel spectrum of the linear "same" convolution.
+
+    scipy's oaconvolve(a, k, mode="same") output i is the full convolution at
+    i + (M-1)//2 for an M-point kernel.  With the kernel placed on a cyclic
+    grid of P >= N + M - 1 - (M-1)//2 points so that its element (M-1)//2
+    sits at the origin, the cyclic convolution equals that output on the N
+    points of the field (no wrap-around reaches them).  The spectrum is the
+    project FFT of that placed kernel.
+    """
+    k = profile.detach().cpu().numpy() if isinstance(profile, torch.Tensor) else np.asarray(profile)
+    k = np.asarray(k, dtype=np.float64)
+    if k.ndim != len(grid):
+        raise ValueError(f"nonlocal kernel of {k.ndim} axes for a {len(grid)}-axis field")
+    pads = tuple(next_pow2(n + m - 1 - (m - 1) // 2) for n, m in zip(grid, k.shape))
+    placed = np.zeros(pads, dtype=np.float64)
+    placed[tuple(slice(0, m) for m in k.shape)] = k
+    placed = np.roll(placed, shift=[-((m - 1) // 2) for m in k.shape], axis=tuple(range(k.ndim)))
+    khat = torch.from_numpy(placed.astype(np.complex128)).to(device=device, dtype=dtype)
+    plan = Plan.get(len(pads), pads, 1, 1, dtype_code(khat), device)
+    plan.fft(khat)
+    return pads, khat.contiguous()
 
 
 def to_device(x, device, dtype=None) -> torch.Tensor:

@@ -270,11 +270,9 @@ class NLSE:
         return 0
 
     def _operator(self, A: torch.Tensor, V, propagator, precision: str,
-                  pump: tuple | None = None) -> OperatorData:
+                  pump: tuple | None = None, plan: Plan | None = None) -> OperatorData:
         if precision not in ("single", "double"):
             raise ValueError("precision must be 'single' or 'double'")
-        if self.nl_length > 0:
-            raise NotImplementedError("nonlocal response (nl_length > 0) is not available yet")
         dev = A.device
         lead = self._lead_shape(tuple(A.shape))
         na = len(self._last_axes)
@@ -300,10 +298,22 @@ class NLSE:
                 vstride = int(np.prod(pix_shape))
             Vd = Vd.contiguous()
         params = torch.from_numpy(self._nl_block(lead, precision, V is not None)).to(dev)
+        khat = None
+        plan = plan if plan is not None else self._build_fft_plan(A)[0]
+        if self.nl_length > 0:
+            # nonlocal response: the reference convolves |A|^2 with nl_profile
+            # ("same" mode) before each nonlinear step (nlse.py:406-408, 444-447)
+            if na == 3:
+                raise NotImplementedError("nonlocal response of 3-D fields")
+            pads, khat = engine.nonlocal_spectrum(self.nl_profile, tuple(A.shape[-na:]), A.dtype,
+                                                  dev)
+            plan.set_nonlocal(pads)
+        else:
+            plan.set_nonlocal(None)
         return OperatorData(prop=prop.contiguous(), params=params,
                             scheme=1 if precision == "double" else 0,
                             rabi=self._rabi_enabled(precision), V=Vd, v_fstride=vstride,
-                            prop_cstride=self._prop_layout(prop), pump=pump)
+                            prop_cstride=self._prop_layout(prop), pump=pump, nl_khat=khat)
 
     def _rabi_enabled(self, precision: str) -> bool:
         return False
@@ -322,7 +332,7 @@ class NLSE:
         A_sq is accepted for signature compatibility; |A|^2 is formed inside
         the fused kernels and never stored.
         """
-        op = self._operator(A, V, propagator, precision)
+        op = self._operator(A, V, propagator, precision, plan=plans[0])
         engine.propagate(plans[0], A, op, 1, 0, graph=False)
 
     # -- pump hooks (DDGPE) ---------------------------------------------------
@@ -378,7 +388,7 @@ class NLSE:
                     raise IndexError(f"the pump time profile has {plen} entries, the loop "
                                      f"runs {n} steps")
                 if n > 0:
-                    op = self._operator(A, V, self.propagator, precision, pump)
+                    op = self._operator(A, V, self.propagator, precision, pump, self.plans[0])
                     engine.propagate(self.plans[0], A, op, n, 0, graph=True)
             else:
                 z_prop = 0
@@ -392,7 +402,8 @@ class NLSE:
                         raise IndexError(f"pump time profile index {i} out of range ({plen})")
                     k = self._op_key()
                     if op is None or k != key:
-                        op = self._operator(A, V, self.propagator, precision, pump)
+                        op = self._operator(A, V, self.propagator, precision, pump,
+                                            self.plans[0])
                         key = k
                     engine.propagate(self.plans[0], A, op, 1, i, graph=False)
                     if isinstance(callback, Callable):

@@ -19,8 +19,6 @@ SKIP = {
 def test_product_matches_reference_fixture(name):
     if name in SKIP:
         pytest.skip(SKIP[name])
-    if "nonlocal" in name:
-        pytest.skip("nonlocal response: separate test module")
     got = gc.run(name, "product")
     ref = gc.load(name)["out"]
     assert got.shape == ref.shape and got.dtype == ref.dtype
