@@ -325,6 +325,31 @@ def run_gb300(args):
         single = {"steps": ng.count_steps(L, DZ), "steps_per_s": ng.count_steps(L, DZ) / min(ts),
                   "note": "one 2048^2 field, 501-step out_field loop from device memory, "
                           "L2 flushed between loops (the field itself fits in L2)"}
+    # the 164-field mixed batch (96 @ 256^2, 48 @ 512^2, 16 @ 1024^2, 4 @ 2048^2), one
+    # grouped graph launch for the whole loop; inputs resident on the device
+    from tests import cases
+
+    jobs = cases.mixed_batch([(96, 256), (48, 512), (16, 1024), (4, 2048)], seed=11 + rank)
+    jobs = [(sim, torch.from_numpy(E).to(dev)) for sim, E in jobs]
+    zb = (args.steps - 0.5) * 5e-5
+    nb = ng.count_steps(zb, 5e-5)
+    ng.out_fields(jobs, zb)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    a.record()
+    ng.out_fields(jobs, zb)
+    b.record()
+    torch.cuda.synchronize()
+    tb = a.elapsed_time(b) / 1e3
+    if dist:
+        tt = torch.tensor([tb], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tb = float(tt.item())
+    mixed = {"fields": 164, "steps": nb, "field_steps_per_s": world * 164 * nb / tb,
+             "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
+                     "and potentials; one CUDA graph with a concurrent branch per grid size"}
     if rank == 0:
         cb, _ = cpu_reference(4, 3, 1)
         cpu_base = cb
@@ -339,7 +364,7 @@ def run_gb300(args):
                            "fields_per_gpu": B, "grid": [N, N], "scheme": "single",
                            "l2": "inputs larger than L2 (256 MiB per GPU)",
                            "step_model_gbs_52B_per_pt": round(step_model_gbs, 1),
-                           "single_field_loop": single},
+                           "single_field_loop": single, "mixed_batch_164": mixed},
                 "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line), flush=True)

@@ -134,6 +134,23 @@ int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nst
                    int64_t step0, int32_t flags, void* stream);
 
 /*
+ * Groups of fields with different geometries advanced together: each group
+ * (its own plan, field and operator) runs its nsteps[i] split steps on a
+ * branch of one CUDA graph, the branches concurrent, so the whole batched
+ * z-loop is one graph launch (replayed when called again with the same
+ * arguments; NLSE_RUN_GRAPH is implied).  The batch of SURVEY-style mixed
+ * grids (e.g. 96 fields at 256^2, 48 at 512^2, 16 at 1024^2, 4 at 2048^2)
+ * is four groups.  No reference counterpart as one call: the reference runs
+ * one out_field per NLSE instance.
+ */
+typedef struct nlse_group_s* nlse_group;
+int nlse_group_create(nlse_group* out);
+int nlse_group_destroy(nlse_group group);
+int nlse_group_propagate(nlse_group group, int32_t ngroups, const nlse_plan* plans,
+                         void* const* fields, const nlse_operator* ops, const int64_t* nsteps,
+                         void* stream);
+
+/*
  * Nonlocal response (the reference's oaconvolve(|A|^2, nl_profile, "same")
  * over the transform axes, NLSE/nlse.py:143-155, 406-408, 444-447 and the
  * CNLSE counterparts): give the plan a zero-padded grid pad_y x pad_x (1-D:

@@ -9,6 +9,7 @@ libnlse_sm103.so (see include/nlse_gb300.h).
 __version__ = "2.3.0+gb300.1"
 
 from . import callbacks
+from .batch import out_fields
 from .callbacks import adapt_delta_z, evaluate_delta_n, norm, sample
 from .cnlse import CNLSE
 from .cnlse_1d import CNLSE_1d
@@ -20,5 +21,5 @@ from .nlse_3d import NLSE_3d
 
 __all__ = [
     "NLSE", "NLSE_1d", "NLSE_3d", "CNLSE", "CNLSE_1d", "GPE", "DDGPE", "callbacks",
-    "sample", "norm", "evaluate_delta_n", "adapt_delta_z", "count_steps",
+    "sample", "norm", "evaluate_delta_n", "adapt_delta_z", "count_steps", "out_fields",
 ]

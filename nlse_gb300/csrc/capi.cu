@@ -661,6 +661,108 @@ int nlse_plan_destroy(nlse_plan p) {
   return NLSE_OK;
 }
 
+}  // extern "C"
+
+struct nlse_group_s {
+  cudaStream_t cap = nullptr;
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> ev;
+  cudaEvent_t fork = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<uint8_t> key;  // serialized arguments of the captured graph
+};
+
+extern "C" {
+
+int nlse_group_create(nlse_group* out) {
+  g_err.clear();
+  if (!out) return fail(NLSE_ERR_ARG, "null argument");
+  auto* g = new nlse_group_s();
+  cudaError_t e = cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    nlse_group_destroy(g);
+    return cuda_fail(e, "group create");
+  }
+  *out = g;
+  return NLSE_OK;
+}
+
+int nlse_group_destroy(nlse_group g) {
+  if (!g) return NLSE_OK;
+  if (g->gexec) cudaGraphExecDestroy(g->gexec);
+  for (auto st : g->branch) cudaStreamDestroy(st);
+  for (auto ev : g->ev) cudaEventDestroy(ev);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->cap) cudaStreamDestroy(g->cap);
+  delete g;
+  return NLSE_OK;
+}
+
+int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* const* fields,
+                         const nlse_operator* ops, const int64_t* nsteps, void* stream) {
+  g_err.clear();
+  if (!g || n <= 0 || !plans || !fields || !ops || !nsteps) return fail(NLSE_ERR_ARG, "null argument");
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i] || !fields[i] || nsteps[i] < 0) return fail(NLSE_ERR_ARG, "group %d: bad entry", i);
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i])
+        return fail(NLSE_ERR_ARG, "groups %d and %d share a plan (its scratch would be raced)", j, i);
+    if (!plans[i]->fft_ok) return fail(NLSE_ERR_UNSUPPORTED, "group %d: transform lengths", i);
+    const int rc = check_op(plans[i], &ops[i]);
+    if (rc != NLSE_OK) return rc;
+  }
+  std::vector<uint8_t> key;
+  auto put = [&](const void* p, size_t b) {
+    const uint8_t* c = static_cast<const uint8_t*>(p);
+    key.insert(key.end(), c, c + b);
+  };
+  put(&n, sizeof(n));
+  put(plans, sizeof(nlse_plan) * n);
+  put(fields, sizeof(void*) * n);
+  put(ops, sizeof(nlse_operator) * n);
+  put(nsteps, sizeof(int64_t) * n);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (!(g->gexec && key == g->key)) {
+    while ((int)g->branch.size() < n) {
+      cudaStream_t st;
+      cudaEvent_t ev;
+      NLSE_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "branch stream");
+      NLSE_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "branch event");
+      g->branch.push_back(st);
+      g->ev.push_back(ev);
+    }
+    cudaGraph_t graph = nullptr;
+    NLSE_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int rc = NLSE_OK;
+    cudaError_t e = cudaEventRecord(g->fork, g->cap);
+    for (int i = 0; i < n && rc == NLSE_OK && e == cudaSuccess; ++i) {
+      e = cudaStreamWaitEvent(g->branch[i], g->fork, 0);
+      if (e != cudaSuccess) break;
+      rc = enqueue_steps(plans[i], fields[i], &ops[i], nsteps[i], 0, g->branch[i]);
+      if (rc != NLSE_OK) break;
+      e = cudaEventRecord(g->ev[i], g->branch[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(g->cap, g->ev[i], 0);
+    }
+    const cudaError_t e2 = cudaStreamEndCapture(g->cap, &graph);
+    if (rc != NLSE_OK || e != cudaSuccess || e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      if (rc != NLSE_OK) return rc;
+      return cuda_fail(e != cudaSuccess ? e : e2, "group capture");
+    }
+    if (g->gexec) {
+      cudaGraphExecDestroy(g->gexec);
+      g->gexec = nullptr;
+    }
+    e = cudaGraphInstantiate(&g->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "group graph instantiate");
+    g->key = key;
+  }
+  NLSE_CUDA(cudaGraphLaunch(g->gexec, s), "group graph launch");
+  return NLSE_OK;
+}
+
 int nlse_plan_status(nlse_plan p, void* stream) {
   g_err.clear();
   if (!p) return fail(NLSE_ERR_ARG, "null plan");

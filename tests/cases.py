@@ -67,3 +67,37 @@ ORACLES = {
     "GPE": orc.OracleGPE,
     "DDGPE": orc.OracleDDGPE,
 }
+
+
+def mixed_batch(groups, seed=0, dtype=np.complex64, cls=None, dz=5e-5):
+    """Seeded mixed batch: for each (count, N) a group of `count` fields on an N x N grid.
+
+    Per field (the 164-field configuration's distributions): power ~ U[0.1, 2] W,
+    n2 = -10^U[-10, -8.4] m^2/W, waist ~ U[0.8, 2.5] mm, potential = sum of 1-8
+    Gaussian wells (depth U[0.5, 2]e-4, width U[30, 150] um, centres uniform in the
+    inner half of the window); Isat = 1e5, alpha = 20, L = 10 mm, dz = 5e-5 m.
+    Returns [(simulation, E_0)], one simulation per group with per-field
+    parameter arrays, as the reference expresses such a batch.
+    """
+    import nlse_gb300 as ng
+
+    cls = cls or ng.NLSE
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for count, N in groups:
+        power = rng.uniform(0.1, 2.0, count)
+        n2 = -(10.0 ** rng.uniform(-10, -8.4, count)).reshape(count, 1, 1)
+        waist = rng.uniform(0.8e-3, 2.5e-3, count)
+        sim = cls(ALPHA, power, WINDOW, n2, None, L, NX=N, NY=N, Isat=ISAT)
+        sim.delta_z = dz
+        V = np.zeros((count, N, N))
+        for b in range(count):
+            for _ in range(rng.integers(1, 9)):
+                depth = rng.uniform(0.5e-4, 2e-4)
+                width = rng.uniform(30e-6, 150e-6)
+                x0, y0 = rng.uniform(-WINDOW / 4, WINDOW / 4, 2)
+                V[b] -= depth * np.exp(-((sim.XX - x0) ** 2 + (sim.YY - y0) ** 2) / width**2)
+        sim.V = V.astype(np.float32)
+        E = np.exp(-(sim.XX[None] ** 2 + sim.YY[None] ** 2) / waist[:, None, None] ** 2)
+        jobs.append((sim, E.astype(dtype)))
+    return jobs
