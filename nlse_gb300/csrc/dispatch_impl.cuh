@@ -30,7 +30,9 @@ static cudaError_t rows_tma_n(const StepArgs& a, cudaStream_t s, bool prep, bool
       *used = true;
       return set_smem(kern, smem);
     }
-    if (!(a.flags & F_IN_BLK) || a.tma_grid <= 0 || !a.tmap) return cudaSuccess;
+    // the kernel indexes lines with 32-bit integers
+    if (!(a.flags & F_IN_BLK) || a.tma_grid <= 0 || !a.tmap || a.nq >= (int64_t(1) << 31))
+      return cudaSuccess;
     *used = true;
     if (a.nq <= 0) return cudaSuccess;
     int per_sm = 0;

@@ -212,6 +212,70 @@ __device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T
   }
 }
 
+// Radix of the pass at stride NS in a transform of N points, E per thread
+// (a butterfly never spans more than a thread's elements).
+template <int N, int E, int NS>
+struct PassRadix {
+  static constexpr int RMAX = E < 16 ? E : 16;
+  static constexpr int R = (N / NS) >= RMAX ? RMAX : (N / NS);
+};
+
+// Number of shared-memory exchanges in one N-point transform.
+__host__ __device__ constexpr int fft_exchanges(int n, int e) {
+  int k = 0;
+  for (int ns = 1;;) {
+    const int rmax = e < 16 ? e : 16;
+    const int r = (n / ns) >= rmax ? rmax : n / ns;
+    if (ns * r >= n) return k;
+    ns *= r;
+    ++k;
+  }
+}
+
+// Exchange halves after the pass at stride NS: every thread stores its
+// butterfly outputs at their Stockham positions, then (after a barrier) loads
+// the elements t + j*TPL of the next pass.
+template <typename T, int N, int E, int NS>
+__device__ __forceinline__ void exchange_store(const cpx<T> (&x)[E], int t, cpx<T>* sm,
+                                               int stride) {
+  constexpr int TPL = N / E;
+  constexpr int R = PassRadix<N, E, NS>::R;
+  constexpr int BPT = E / R;
+#pragma unroll
+  for (int s = 0; s < BPT; ++s) {
+    const int b = t + s * TPL;
+    const int base = (b / NS) * NS * R + (b & (NS - 1));
+    // padi(base + r*NS) as one computed base plus compile-time offsets
+    // whenever the 16-element padding groups allow it
+    if constexpr (NS % 16 == 0) {
+      const int pb = padi(base) * stride;
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[pb + r * (NS + NS / 16) * stride] = x[s + r * BPT];
+    } else if constexpr (NS == 1 && R == 16) {
+      const int pb = (17 * b) * stride;  // padi(16 b + r) = 17 b + r
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[pb + r * stride] = x[s + r * BPT];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[padi(base + r * NS) * stride] = x[s + r * BPT];
+    }
+  }
+}
+
+template <typename T, int N, int E>
+__device__ __forceinline__ void exchange_load(cpx<T> (&x)[E], int t, const cpx<T>* sm,
+                                              int stride) {
+  constexpr int TPL = N / E;
+  if constexpr (TPL % 16 == 0) {
+    const int pb = padi(t) * stride;  // padi(t + j TPL) = padi(t) + j (TPL + TPL/16)
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sm[pb + j * (TPL + TPL / 16) * stride];
+  } else {
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sm[padi(t + j * TPL) * stride];
+  }
+}
+
 // Full N-point transform of one line.  sm points at the line's padded shared
 // buffer; element i lives at sm[padi(i) * STRIDE] (STRIDE > 1 interleaves W
 // column lines, the caller offsets sm by the column).  All threads of the
@@ -219,11 +283,8 @@ __device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T
 template <typename T, int N, int E, int NS, bool INV>
 __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
                                          const cpx<T>* __restrict__ tw) {
-  constexpr int TPL = N / E;
-  constexpr int RMAX = E < 16 ? E : 16;  // a butterfly never spans more than a thread's elements
-  constexpr int R = (N / NS) >= RMAX ? RMAX : (N / NS);
-  constexpr int BPT = E / R;
-  static_assert(BPT >= 1 && BPT * R == E, "radix must divide the elements per thread");
+  constexpr int R = PassRadix<N, E, NS>::R;
+  static_assert((E / R) * R == E, "radix must divide the elements per thread");
   if constexpr (NS == 1) {
     // Recompute the shared-memory addresses in every transform instead of
     // keeping those of an earlier transform in this kernel live in registers.
@@ -232,35 +293,34 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
   stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
   if constexpr (NS * R < N) {
     __syncthreads();
-#pragma unroll
-    for (int s = 0; s < BPT; ++s) {
-      const int b = t + s * TPL;
-      const int base = (b / NS) * NS * R + (b & (NS - 1));
-      // padi(base + r*NS) as one computed base plus compile-time offsets
-      // whenever the 16-element padding groups allow it
-      if constexpr (NS % 16 == 0) {
-        const int pb = padi(base) * stride;
-#pragma unroll
-        for (int r = 0; r < R; ++r) sm[pb + r * (NS + NS / 16) * stride] = x[s + r * BPT];
-      } else if constexpr (NS == 1 && R == 16) {
-        const int pb = (17 * b) * stride;  // padi(16 b + r) = 17 b + r
-#pragma unroll
-        for (int r = 0; r < R; ++r) sm[pb + r * stride] = x[s + r * BPT];
-      } else {
-#pragma unroll
-        for (int r = 0; r < R; ++r) sm[padi(base + r * NS) * stride] = x[s + r * BPT];
-      }
-    }
+    exchange_store<T, N, E, NS>(x, t, sm, stride);
     __syncthreads();
-    if constexpr (TPL % 16 == 0) {
-      const int pb = padi(t) * stride;  // padi(t + j TPL) = padi(t) + j (TPL + TPL/16)
-#pragma unroll
-      for (int j = 0; j < E; ++j) x[j] = sm[pb + j * (TPL + TPL / 16) * stride];
-    } else {
-#pragma unroll
-      for (int j = 0; j < E; ++j) x[j] = sm[padi(t + j * TPL) * stride];
-    }
+    exchange_load<T, N, E>(x, t, sm, stride);
     fft_line<T, N, E, NS * R, INV>(x, t, sm, stride, tw);
+  }
+}
+
+// fft_line with two exchange buffers used alternately (A for the first
+// exchange, then B, A, ...), one barrier per exchange instead of two.
+// Caller contract: when the transform starts, no thread still reads A or B
+// from an earlier use unless a barrier has passed since; with an even number
+// of exchanges the last one uses B, so A is free once the transform returns.
+// FENCE_A: order the generic-proxy stores into A before later bulk copies
+// (A is a bulk-copy staging buffer that is refilled afterwards).
+template <typename T, int N, int E, int NS, bool INV, int P, bool FENCE_A>
+__device__ __forceinline__ void fft_line_db(cpx<T> (&x)[E], int t, cpx<T>* smA, cpx<T>* smB,
+                                            int stride, const cpx<T>* __restrict__ tw) {
+  constexpr int R = PassRadix<N, E, NS>::R;
+  static_assert((E / R) * R == E, "radix must divide the elements per thread");
+  if constexpr (NS == 1) asm volatile("" : "+r"(t)::"memory");
+  stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
+  if constexpr (NS * R < N) {
+    cpx<T>* sm = P ? smB : smA;
+    exchange_store<T, N, E, NS>(x, t, sm, stride);
+    if constexpr (FENCE_A && P == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    exchange_load<T, N, E>(x, t, sm, stride);
+    fft_line_db<T, N, E, NS * R, INV, P ^ 1, FENCE_A>(x, t, smA, smB, stride, tw);
   }
 }
 

@@ -132,11 +132,15 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 
 // ---- exp(re) * (cos(im), sin(im)) ------------------------------------------
 // The split step's per-step arguments are small (|re| = alpha*sat*dz,
-// |im| = phase per step), so the common case uses truncated Maclaurin series
-// of exp, sin and cos (Horner form), with enough terms that the truncation
-// error is far below one unit in the last place on the stated range:
-//   float:  |re| <= 1/16 (exp to x^7), |im| <= 1/2 (sin to x^11, cos to x^12)
-//   double: |re| <= 1/32 (exp to x^12), |im| <= 1/4 (sin to x^19, cos to x^20)
+// |im| = phase per step), so the common case evaluates truncated Maclaurin
+// polynomials of exp, sin and cos in Horner form with the coefficients 1/k!
+// (one FMA per term).  The degrees are chosen so that the first omitted term
+// is far below one unit in the last place on the range:
+//   float:  |re| <= 1/16: exp to x^5 (next term < 1e-10);
+//           |im| <= 1/4:  sin to x^7 (< 1e-11), cos to x^8 (< 3e-13)
+//   double: |re| <= 1/32: exp to x^8 (< 3e-17);
+//           |im| <= 1/4:  sin to x^11 (< 3e-18), cos to x^12 (< 2e-19)
+// sin is formed as im + (im*x^2)*p(x^2), so its leading term is exact.
 // Outside the range the CUDA library functions are called from a non-inlined
 // helper, which keeps the unrolled kernels small.
 static __device__ __noinline__ void cis_exp_lib(float re, float im, float* cr, float* ci) {
@@ -154,37 +158,45 @@ static __device__ __noinline__ void cis_exp_lib(double re, double im, double* cr
   *ci = e * sn;
 }
 
+// 1/k! and (-1)^k/(2k+1)!, (-1)^k/(2k)! evaluated in double at compile time
+__host__ __device__ constexpr double inv_fact(int k) {
+  double r = 1.0;
+  for (int i = 2; i <= k; ++i) r /= i;
+  return r;
+}
+__host__ __device__ constexpr double sin_coef(int k) {  // coefficient of x^(2k+1)
+  return (k % 2 ? -1.0 : 1.0) * inv_fact(2 * k + 1);
+}
+__host__ __device__ constexpr double cos_coef(int k) {  // coefficient of x^(2k)
+  return (k % 2 ? -1.0 : 1.0) * inv_fact(2 * k);
+}
+
 template <typename T> struct CisRange;
 template <> struct CisRange<float> {
-  static constexpr float RE = 0.0625f, IM = 0.5f;
-  static constexpr int EXP_TERMS = 8, SIN_TERMS = 6, COS_TERMS = 7;
+  static constexpr float RE = 0.0625f, IM = 0.25f;
+  static constexpr int EXP_DEG = 5, SIN_K = 3, COS_K = 4;  // sin to x^(2*3+1), cos to x^(2*4)
 };
 template <> struct CisRange<double> {
   static constexpr double RE = 0.03125, IM = 0.25;
-  static constexpr int EXP_TERMS = 13, SIN_TERMS = 10, COS_TERMS = 11;
+  static constexpr int EXP_DEG = 8, SIN_K = 5, COS_K = 6;
 };
 
 template <typename T>
 __device__ __forceinline__ void cis_exp(T re, T im, T* cr, T* ci) {
   using R = CisRange<T>;
   if (fabs(re) <= R::RE && fabs(im) <= R::IM) {
-    // exp(re) = 1 + re (1 + re/2 (1 + re/3 (...)))
-    // (the factors 1/k are compile-time constants; only the first two, 1 and
-    // 1/2, matter at the last bit and both are exact)
-    T e = T(1);
+    T e = T(inv_fact(R::EXP_DEG));
 #pragma unroll
-    for (int k = R::EXP_TERMS - 1; k >= 1; --k) e = fma(re * T(1.0 / k), e, T(1));
-    // sin(x) = x (1 - x^2/(2*3) (1 - x^2/(4*5) (...))), cos(x) = 1 - x^2/(1*2) (...)
+    for (int k = R::EXP_DEG - 1; k >= 0; --k) e = fma(e, re, T(inv_fact(k)));
     const T x2 = im * im;
-    T sn = T(1), cs = T(1);
+    T s = T(sin_coef(R::SIN_K));
 #pragma unroll
-    for (int k = R::SIN_TERMS - 1; k >= 1; --k)
-      sn = fma(x2 * T(-1.0 / ((2 * k) * (2 * k + 1))), sn, T(1));
-    sn *= im;
+    for (int k = R::SIN_K - 1; k >= 1; --k) s = fma(s, x2, T(sin_coef(k)));
+    const T sn = fma(im * x2, s, im);
+    T c = T(cos_coef(R::COS_K));
 #pragma unroll
-    for (int k = R::COS_TERMS - 1; k >= 1; --k)
-      cs = fma(x2 * T(-1.0 / ((2 * k - 1) * (2 * k))), cs, T(1));
-    *cr = e * cs;
+    for (int k = R::COS_K - 1; k >= 0; --k) c = fma(c, x2, T(cos_coef(k)));
+    *cr = e * c;
     *ci = e * sn;
   } else {
     cis_exp_lib(re, im, cr, ci);
@@ -479,12 +491,22 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
 // of W elements; the 4-D map {2W scalars, NY, N/W, slabs} with a box of one
 // row and up to 256 runs lands the row in shared memory in natural order.
 // Two stages: row q+grid is in flight while row q is transformed.
+// Elements of one staging line or tile: the padded exchange length rounded up
+// so that every staging buffer starts on a 128-byte boundary (the alignment a
+// tensor-map copy needs for its shared-memory destination).
+template <typename T>
+__host__ __device__ constexpr int stage_len(int n) {
+  constexpr int q = 128 / (int)sizeof(cpx<T>);
+  return (n + q - 1) / q * q;
+}
+
 constexpr int kRowStages = 2;
 
 template <typename T, int N, int NC>
 __host__ __device__ constexpr size_t rows_tma_smem() {
-  return (size_t)kRowStages * NC * N * sizeof(cpx<T>) +
-         (size_t)NC * padded_len(N) * sizeof(cpx<T>) + kRowStages * sizeof(uint64_t);
+  // kRowStages staging lines and one exchange line per component, each padded
+  return (size_t)(kRowStages + 1) * NC * stage_len<T>(padded_len(N)) * sizeof(cpx<T>) +
+         kRowStages * sizeof(uint64_t);
 }
 
 template <typename T, int N, int E, int MODE, int NC>
@@ -496,28 +518,45 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   constexpr unsigned ROW_BYTES = N * sizeof(C);
   constexpr int SL = padded_len(N);
   constexpr bool two = NC == 2;
+  // With an even number of exchanges per transform, the staging line just
+  // read into registers is the transforms' first exchange buffer and is
+  // refilled after them (see fft_line_db); otherwise it is refilled at once.
+  constexpr int NEX = fft_exchanges(N, E);
+  constexpr bool DB = NEX > 0 && NEX % 2 == 0;
   extern __shared__ __align__(128) unsigned char smraw[];
+  constexpr int SLS = stage_len<T>(SL);  // stride of the staging and exchange lines
+  static_assert((SLS * sizeof(C)) % 128 == 0 && (BOXB * W * sizeof(C)) % 128 == 0,
+                "tensor-map copies need 128-byte aligned shared destinations");
   C* stage = reinterpret_cast<C*>(smraw);
-  C* xch = stage + kRowStages * NC * N;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + NC * SL);
+  C* xch = stage + kRowStages * NC * SLS;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + NC * SLS);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int comp = threadIdx.x / TPL, t = threadIdx.x % TPL;
-  const int64_t nq = a.nq;
+  // line indices fit 32 bits (checked when the kernel is chosen), so the
+  // per-line division below is a 32-bit one
+  const unsigned nq = (unsigned)a.nq;
 
   // pixel-line q = (line y, field f) with the field fastest: CTAs of one wave
   // take the same line of all fields and share its potential values in L2
-  const int64_t nf = nq / a.lines_per_comp;
-  auto q_f = [&](int64_t q) { return q % nf; };
-  auto q_y = [&](int64_t q) { return q / nf; };
-  auto issue = [&](int st, int64_t q) {
-    const int64_t f = q_f(q), y = q_y(q);
+  const unsigned nf = nq / (unsigned)a.lines_per_comp;
+  auto q_f = [&](unsigned q) { return q % nf; };
+  auto q_y = [&](unsigned q) { return q / nf; };
+  auto issue = [&](int st, unsigned q) {
+    const unsigned f = q_f(q), y = q_y(q);
     mbar_arrive_expect_tx(&bar[st], NC * ROW_BYTES);
 #pragma unroll
     for (int cc = 0; cc < NC; ++cc)
 #pragma unroll
       for (int bx = 0; bx < NBOX; ++bx)
-        tensor_load_4d(stage + (st * NC + cc) * N + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
+        tensor_load_4d(stage + (st * NC + cc) * SLS + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
                        (int)(f * NC + cc), &bar[st]);
+  };
+  auto refill = [&](int st, unsigned q) {
+    const unsigned qn = q + (unsigned)kRowStages * gridDim.x;
+    if (qn < nq) {
+      fence_proxy_async_smem();
+      issue(st, qn);
+    }
   };
 
   if (threadIdx.x == 0) {
@@ -527,12 +566,12 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int st = 0; st < kRowStages; ++st) {
-      const int64_t q = blockIdx.x + (int64_t)st * gridDim.x;
+      const unsigned q = blockIdx.x + (unsigned)st * gridDim.x;
       if (q < nq) issue(st, q);
     }
   }
   int it = 0;
-  for (int64_t q = blockIdx.x; q < nq; q += gridDim.x, ++it) {
+  for (unsigned q = blockIdx.x; q < nq; q += gridDim.x, ++it) {
     const int st = it % kRowStages;
     const unsigned par = (it / kRowStages) & 1;
     const bool ok = mbar_wait_bounded(&bar[st], par);
@@ -545,9 +584,9 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       return;
     }
     const int64_t f = q_f(q), m = q_y(q);
-    const int64_t pix0 = m * N + t;
+    const int64_t pix0 = m * (int64_t)N + t;
     C x[E], xo[E];
-    const C* sp = stage + (st * NC + comp) * N + t;
+    const C* sp = stage + (st * NC + comp) * SLS + t;
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sp[j * TPL];
     VPre<E> vpre;
@@ -558,15 +597,14 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       for (int j = 0; j < E; ++j) vpre.v[j] = __ldg(vp + j * TPL);
     }
     __syncthreads();  // every thread has read stage st
-    if (threadIdx.x == 0) {
-      const int64_t qn = q + (int64_t)kRowStages * gridDim.x;
-      if (qn < nq) {
-        fence_proxy_async_smem();
-        issue(st, qn);
-      }
+    C* xl = xch + comp * SLS;
+    C* sA = stage + (st * NC + comp) * SLS;
+    if constexpr (DB) {
+      fft_line_db<T, N, E, 1, true, 0, true>(x, t, sA, xl, 1, tw);
+    } else {
+      if (threadIdx.x == 0) refill(st, q);
+      fft_line<T, N, E, 1, true>(x, t, xl, 1, tw);
     }
-    C* xl = xch + comp * SL;
-    fft_line<T, N, E, 1, true>(x, t, xl, 1, tw);
     const T sc = T(a.inv_n);
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], sc);
@@ -580,7 +618,11 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
         if (two) exchange_partner<T, N, E>(x, xo, xch, comp, t);
         nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
       }
-      fft_line<T, N, E, 1, false>(x, t, xl, 1, tw);
+      // FFT 2 starts with stage st again: its last reads there (FFT 1) are
+      // behind FFT 1's final barrier, and xch's (partner exchange) behind
+      // FFT 2's first one
+      if constexpr (DB) fft_line_db<T, N, E, 1, false, 0, true>(x, t, sA, xl, 1, tw);
+      else fft_line<T, N, E, 1, false>(x, t, xl, 1, tw);
       C* dst = reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
       const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
 #pragma unroll
@@ -589,6 +631,11 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       C* dst = reinterpret_cast<C*>(a.A) + slab + m * N + t;
 #pragma unroll
       for (int j = 0; j < E; ++j) dst[j * TPL] = x[j];
+    }
+    // the last exchange of the last transform used xch: every read of stage st
+    // is behind a barrier
+    if constexpr (DB) {
+      if (threadIdx.x == 0) refill(st, q);
     }
   }
 }
@@ -665,19 +712,27 @@ constexpr int kColStages = 2;
 
 template <typename T, int N>
 __host__ __device__ constexpr size_t cols_tma_smem() {
-  return (size_t)kColStages * N * BlkW<T>::W * sizeof(cpx<T>) +
-         (size_t)padded_len(N) * BlkW<T>::W * sizeof(cpx<T>) + kColStages * sizeof(uint64_t);
+  // kColStages staging tiles and one exchange tile, each padded
+  return (size_t)(kColStages + 1) * stage_len<T>(padded_len(N) * BlkW<T>::W) * sizeof(cpx<T>) +
+         kColStages * sizeof(uint64_t);
 }
 
 template <typename T, int N, int E, bool PC128>
 __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const ColArgs a) {
   using C = cpx<T>;
   constexpr int TPL = N / E, W = BlkW<T>::W, TILE = N * W;
+  constexpr int SLW = stage_len<T>(padded_len(N) * W);  // one padded tile, 128-byte multiple
+  static_assert((SLW * sizeof(C)) % 128 == 0, "bulk copies need aligned shared destinations");
   constexpr unsigned TILE_BYTES = TILE * sizeof(C);
+  // With an even number of exchanges per transform, the staging tile just
+  // read into registers is the transforms' second exchange buffer and is
+  // refilled after them; otherwise it is refilled at once.
+  constexpr int NEX = fft_exchanges(N, E);
+  constexpr bool DB = NEX > 0 && NEX % 2 == 0;
   extern __shared__ __align__(128) unsigned char smraw[];
   C* stage = reinterpret_cast<C*>(smraw);
-  C* xch = stage + kColStages * TILE;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + padded_len(N) * W);
+  C* xch = stage + kColStages * SLW;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + SLW);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   C* S = reinterpret_cast<C*>(a.A);
   const int c = threadIdx.x % W, t = threadIdx.x / W;
@@ -700,10 +755,18 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
       const int64_t i = blockIdx.x + (int64_t)st * gridDim.x;
       if (i < ntiles) {
         mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
-        bulk_load(stage + st * TILE, tile_ptr(i), TILE_BYTES, &bar[st]);
+        bulk_load(stage + st * SLW, tile_ptr(i), TILE_BYTES, &bar[st]);
       }
     }
   }
+  auto refill = [&](int st, int64_t i) {
+    const int64_t inext = i + (int64_t)kColStages * gridDim.x;
+    if (inext < ntiles) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+      bulk_load(stage + st * SLW, tile_ptr(inext), TILE_BYTES, &bar[st]);
+    }
+  };
   int it = 0;
   for (int64_t i = blockIdx.x; i < ntiles; i += gridDim.x, ++it) {
     const int st = it % kColStages;
@@ -720,7 +783,7 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
       return;
     }
     C x[E];
-    const C* sp = stage + st * TILE + t * W + c;
+    const C* sp = stage + st * SLW + t * W + c;
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sp[j * TPL * W];
     const int64_t o = tile_o(i);
@@ -733,15 +796,13 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
       for (int j = 0; j < E; ++j) pre[j] = __ldg(reinterpret_cast<const float2*>(a.prop) + pb + j * TPL * W);
     }
     __syncthreads();  // every thread has read stage st
-    if (threadIdx.x == 0) {
-      const int64_t inext = i + (int64_t)kColStages * gridDim.x;
-      if (inext < ntiles) {
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
-        bulk_load(stage + st * TILE, tile_ptr(inext), TILE_BYTES, &bar[st]);
-      }
+    C* sA = stage + st * SLW + c;
+    if constexpr (DB) {
+      fft_line_db<T, N, E, 1, false, 0, true>(x, t, sA, xch + c, W, tw);
+    } else {
+      if (threadIdx.x == 0) refill(st, i);
+      fft_line<T, N, E, 1, false>(x, t, xch + c, W, tw);
     }
-    fft_line<T, N, E, 1, false>(x, t, xch + c, W, tw);
     if constexpr (PC128) {
 #pragma unroll
       for (int j = 0; j < E; ++j) x[j] = mul_prop<T, true>(x[j], a.prop, pb + j * TPL * W);
@@ -749,7 +810,13 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
 #pragma unroll
       for (int j = 0; j < E; ++j) x[j] = cmul<T>(x[j], mk<T>(T(pre[j].x), T(pre[j].y)));
     }
-    fft_line<T, N, E, 1, true>(x, t, xch + c, W, tw);
+    if constexpr (DB) {
+      fft_line_db<T, N, E, 1, true, 0, true>(x, t, sA, xch + c, W, tw);
+      // the last exchange used xch, so every read of stage st is behind a barrier
+      if (threadIdx.x == 0) refill(st, i);
+    } else {
+      fft_line<T, N, E, 1, true>(x, t, xch + c, W, tw);
+    }
     C* g = S + o * a.outer_stride + toff;
 #pragma unroll
     for (int j = 0; j < E; ++j) g[j * TPL * W] = x[j];
