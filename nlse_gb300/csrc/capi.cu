@@ -281,6 +281,7 @@ StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
   a.nq = d.nfields * a.lines_per_comp;
   a.pix = p->pix;
   a.inv_n = 1.0 / (double)p->pix;
+  a.inv_nf = (float)a.inv_n;
   a.comps = d.comps;
   a.nsteps = 1;
   if (op) {

@@ -280,7 +280,15 @@ __device__ __forceinline__ void exchange_load(cpx<T> (&x)[E], int t, const cpx<T
 // buffer; element i lives at sm[padi(i) * STRIDE] (STRIDE > 1 interleaves W
 // column lines, the caller offsets sm by the column).  All threads of the
 // CTA must call this (it contains __syncthreads).
-template <typename T, int N, int E, int NS, bool INV>
+// Order this thread's generic-proxy shared-memory stores before later bulk
+// copies (async proxy) into the same buffer.
+__device__ __forceinline__ void fence_async_after_stores() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// FENCE: the exchange buffer is also a bulk-copy staging buffer that is
+// refilled later, so the exchange stores are fenced against that copy.
+template <typename T, int N, int E, int NS, bool INV, bool FENCE = false>
 __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
                                          const cpx<T>* __restrict__ tw) {
   constexpr int R = PassRadix<N, E, NS>::R;
@@ -294,9 +302,10 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
   if constexpr (NS * R < N) {
     __syncthreads();
     exchange_store<T, N, E, NS>(x, t, sm, stride);
+    if constexpr (FENCE) fence_async_after_stores();
     __syncthreads();
     exchange_load<T, N, E>(x, t, sm, stride);
-    fft_line<T, N, E, NS * R, INV>(x, t, sm, stride, tw);
+    fft_line<T, N, E, NS * R, INV, FENCE>(x, t, sm, stride, tw);
   }
 }
 
@@ -305,9 +314,9 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
 // Caller contract: when the transform starts, no thread still reads A or B
 // from an earlier use unless a barrier has passed since; with an even number
 // of exchanges the last one uses B, so A is free once the transform returns.
-// FENCE_A: order the generic-proxy stores into A before later bulk copies
-// (A is a bulk-copy staging buffer that is refilled afterwards).
-template <typename T, int N, int E, int NS, bool INV, int P, bool FENCE_A>
+// FM: bit 0 / bit 1 fence the stores into A / B (buffers that later receive
+// bulk copies).
+template <typename T, int N, int E, int NS, bool INV, int P, int FM>
 __device__ __forceinline__ void fft_line_db(cpx<T> (&x)[E], int t, cpx<T>* smA, cpx<T>* smB,
                                             int stride, const cpx<T>* __restrict__ tw) {
   constexpr int R = PassRadix<N, E, NS>::R;
@@ -317,10 +326,33 @@ __device__ __forceinline__ void fft_line_db(cpx<T> (&x)[E], int t, cpx<T>* smA, 
   if constexpr (NS * R < N) {
     cpx<T>* sm = P ? smB : smA;
     exchange_store<T, N, E, NS>(x, t, sm, stride);
-    if constexpr (FENCE_A && P == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if constexpr ((FM >> P) & 1) fence_async_after_stores();
     __syncthreads();
     exchange_load<T, N, E>(x, t, sm, stride);
-    fft_line_db<T, N, E, NS * R, INV, P ^ 1, FENCE_A>(x, t, smA, smB, stride, tw);
+    fft_line_db<T, N, E, NS * R, INV, P ^ 1, FM>(x, t, smA, smB, stride, tw);
+  }
+}
+
+// fft_line on one buffer whose first exchange needs no leading barrier (the
+// caller guarantees that no thread still reads sm), with hook() run by every
+// thread right after that exchange's barrier: at that point every read of
+// shared memory the caller issued before the transform has completed.
+template <typename T, int N, int E, bool INV, bool FENCE, typename Hook>
+__device__ __forceinline__ void fft_line_hook(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
+                                              const cpx<T>* __restrict__ tw, Hook&& hook) {
+  constexpr int R = PassRadix<N, E, 1>::R;
+  static_assert((E / R) * R == E, "radix must divide the elements per thread");
+  asm volatile("" : "+r"(t)::"memory");
+  stockham_pass<T, N, E, R, 1, INV>(x, t, tw);
+  if constexpr (R < N) {
+    exchange_store<T, N, E, 1>(x, t, sm, stride);
+    if constexpr (FENCE) fence_async_after_stores();
+    __syncthreads();
+    hook();
+    exchange_load<T, N, E>(x, t, sm, stride);
+    fft_line<T, N, E, R, INV, FENCE>(x, t, sm, stride, tw);
+  } else {
+    hook();
   }
 }
 

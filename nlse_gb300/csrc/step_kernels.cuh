@@ -73,6 +73,7 @@ struct StepArgs {
   int64_t v_fstride;        // field stride of V (0: shared)
   int64_t prop_cstride;     // component stride of the propagator
   double inv_n;             // 1 / (number of pixels), inverse-FFT normalisation
+  float inv_nf;             // the same in FP32 (exact: a power of two)
   int comps;                // 1 or 2
   int step;                 // step index (pump time profile)
   int nsteps;               // steps fused inside one launch (1-D full mode)
@@ -230,6 +231,12 @@ __device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>&
   T cr, ci;
   cis_exp<T>(re, im, &cr, &ci);
   return cmul<T>(A, mk<T>(cr, ci));
+}
+
+template <typename T>
+__device__ __forceinline__ T inv_n_of(const StepArgs& a) {
+  if constexpr (std::is_same<T, float>::value) return a.inv_nf;
+  else return a.inv_n;
 }
 
 template <typename T>
@@ -460,7 +467,7 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
       fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
     } else {
       fft_line<T, N, E, 1, true>(x, t, sml, 1, tw);
-      const T s = T(a.inv_n);
+      const T s = inv_n_of<T>(a);
 #pragma unroll
       for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], s);
       if constexpr (MODE != ROW_INV) {
@@ -504,8 +511,12 @@ constexpr int kRowStages = 2;
 
 template <typename T, int N, int NC>
 __host__ __device__ constexpr size_t rows_tma_smem() {
-  // kRowStages staging lines and one exchange line per component, each padded
-  return (size_t)(kRowStages + 1) * NC * stage_len<T>(padded_len(N)) * sizeof(cpx<T>) +
+  // per component: two line buffers that alternate as staging and exchange
+  // buffers (an even number of exchanges per transform), else kRowStages
+  // staging lines and one exchange line; each padded
+  constexpr int nex = fft_exchanges(N, Shape<N>::E);
+  constexpr int nbuf = (nex > 0 && nex % 2 == 0) ? 2 : kRowStages + 1;
+  return (size_t)nbuf * NC * stage_len<T>(padded_len(N)) * sizeof(cpx<T>) +
          kRowStages * sizeof(uint64_t);
 }
 
@@ -518,18 +529,23 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   constexpr unsigned ROW_BYTES = N * sizeof(C);
   constexpr int SL = padded_len(N);
   constexpr bool two = NC == 2;
-  // With an even number of exchanges per transform, the staging line just
-  // read into registers is the transforms' first exchange buffer and is
-  // refilled after them (see fft_line_db); otherwise it is refilled at once.
+  static_assert(E == Shape<N>::E, "shared-memory size assumes Shape<N>::E");
+  // DB (an even number of exchanges per transform): two buffers X0, X1 of NC
+  // lines.  Line i arrives in X[i&1] by a tensor-map copy; its transforms use
+  // X[i&1] (A) and X[(i+1)&1] (B) as exchange buffers, the forward transform
+  // only A, and B receives line i+1 as soon as the forward transform's first
+  // barrier has passed.  Otherwise: a two-stage staging ring X0, X1, refilled
+  // as soon as read, and the exchange buffer X2.
   constexpr int NEX = fft_exchanges(N, E);
   constexpr bool DB = NEX > 0 && NEX % 2 == 0;
+  constexpr int NBUF = DB ? 2 : kRowStages + 1;
   extern __shared__ __align__(128) unsigned char smraw[];
-  constexpr int SLS = stage_len<T>(SL);  // stride of the staging and exchange lines
+  constexpr int SLS = stage_len<T>(SL);  // stride of the line buffers
   static_assert((SLS * sizeof(C)) % 128 == 0 && (BOXB * W * sizeof(C)) % 128 == 0,
                 "tensor-map copies need 128-byte aligned shared destinations");
-  C* stage = reinterpret_cast<C*>(smraw);
-  C* xch = stage + kRowStages * NC * SLS;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + NC * SLS);
+  C* X = reinterpret_cast<C*>(smraw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(X + NBUF * NC * SLS);
+  auto buf = [&](int b, int cc) { return X + (b * NC + cc) * SLS; };
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int comp = threadIdx.x / TPL, t = threadIdx.x % TPL;
   // line indices fit 32 bits (checked when the kernel is chosen), so the
@@ -541,21 +557,21 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   const unsigned nf = nq / (unsigned)a.lines_per_comp;
   auto q_f = [&](unsigned q) { return q % nf; };
   auto q_y = [&](unsigned q) { return q / nf; };
-  auto issue = [&](int st, unsigned q) {
+  auto issue = [&](int b, unsigned q) {
     const unsigned f = q_f(q), y = q_y(q);
-    mbar_arrive_expect_tx(&bar[st], NC * ROW_BYTES);
+    mbar_arrive_expect_tx(&bar[b], NC * ROW_BYTES);
 #pragma unroll
     for (int cc = 0; cc < NC; ++cc)
 #pragma unroll
       for (int bx = 0; bx < NBOX; ++bx)
-        tensor_load_4d(stage + (st * NC + cc) * SLS + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
-                       (int)(f * NC + cc), &bar[st]);
+        tensor_load_4d(buf(b, cc) + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
+                       (int)(f * NC + cc), &bar[b]);
   };
-  auto refill = [&](int st, unsigned q) {
-    const unsigned qn = q + (unsigned)kRowStages * gridDim.x;
+  // load line qn into buffer b once every generic access to b is complete
+  auto prefetch = [&](int b, unsigned qn) {
     if (qn < nq) {
       fence_proxy_async_smem();
-      issue(st, qn);
+      issue(b, qn);
     }
   };
 
@@ -565,30 +581,32 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int st = 0; st < kRowStages; ++st) {
+    constexpr int first = DB ? 1 : kRowStages;
+    for (int st = 0; st < first; ++st) {
       const unsigned q = blockIdx.x + (unsigned)st * gridDim.x;
       if (q < nq) issue(st, q);
     }
   }
   int it = 0;
   for (unsigned q = blockIdx.x; q < nq; q += gridDim.x, ++it) {
-    const int st = it % kRowStages;
-    const unsigned par = (it / kRowStages) & 1;
+    const int st = it & 1;  // kRowStages == 2
+    const unsigned par = (it >> 1) & 1;
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
+      // give up: record it, let the copies in flight land (bounded), leave
       if (threadIdx.x == 0) {
         atomicExch(a.status, DEV_WAIT_TIMEOUT);
         mbar_wait_bounded(&bar[st], par);
-        if (q + gridDim.x < nq) mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kRowStages) & 1);
+        if (!DB && q + gridDim.x < nq) mbar_wait_bounded(&bar[st ^ 1], ((it + 1) >> 1) & 1);
       }
       return;
     }
     const int64_t f = q_f(q), m = q_y(q);
     const int64_t pix0 = m * (int64_t)N + t;
     C x[E], xo[E];
-    const C* sp = stage + (st * NC + comp) * SLS + t;
+    C* sA = buf(st, comp);
 #pragma unroll
-    for (int j = 0; j < E; ++j) x[j] = sp[j * TPL];
+    for (int j = 0; j < E; ++j) x[j] = sA[t + j * TPL];
     VPre<E> vpre;
     vpre.on = (a.flags & F_HAS_V) && (a.flags & F_V_F32) && !(a.flags & F_V_COMPLEX);
     if (vpre.on) {
@@ -596,46 +614,57 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
 #pragma unroll
       for (int j = 0; j < E; ++j) vpre.v[j] = __ldg(vp + j * TPL);
     }
-    __syncthreads();  // every thread has read stage st
-    C* xl = xch + comp * SLS;
-    C* sA = stage + (st * NC + comp) * SLS;
+    __syncthreads();  // every thread has read its line from buffer st
+    const int bB = DB ? (st ^ 1) : kRowStages;
+    C* sB = buf(bB, comp);   // second exchange buffer
+    C* xpart = buf(bB, 0);   // partner exchange region (NC lines)
     if constexpr (DB) {
-      fft_line_db<T, N, E, 1, true, 0, true>(x, t, sA, xl, 1, tw);
+      fft_line_db<T, N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
     } else {
-      if (threadIdx.x == 0) refill(st, q);
-      fft_line<T, N, E, 1, true>(x, t, xl, 1, tw);
+      if (threadIdx.x == 0) prefetch(st, q + (unsigned)kRowStages * gridDim.x);
+      fft_line<T, N, E, 1, true>(x, t, sB, 1, tw);
     }
-    const T sc = T(a.inv_n);
+    const T sc = inv_n_of<T>(a);
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], sc);
     if (!(a.flags & F_NO_POST)) {
-      if (two) exchange_partner<T, N, E>(x, xo, xch, comp, t);
+      if (two) {
+        exchange_partner<T, N, E>(x, xo, xpart, comp, t);
+        if (DB) fence_proxy_async_smem();
+      }
       nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true, &vpre);
     }
     const int64_t slab = (f * NC + comp) * a.pix;
     if constexpr (MODE == ROW_INV_NL_FWD) {
       if (a.flags & F_PRE_NL) {
-        if (two) exchange_partner<T, N, E>(x, xo, xch, comp, t);
+        if (two) {
+          exchange_partner<T, N, E>(x, xo, xpart, comp, t);
+          if (DB) fence_proxy_async_smem();
+        }
         nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
       }
-      // FFT 2 starts with stage st again: its last reads there (FFT 1) are
-      // behind FFT 1's final barrier, and xch's (partner exchange) behind
-      // FFT 2's first one
-      if constexpr (DB) fft_line_db<T, N, E, 1, false, 0, true>(x, t, sA, xl, 1, tw);
-      else fft_line<T, N, E, 1, false>(x, t, xl, 1, tw);
+      if constexpr (DB) {
+        // forward transform in A alone: A's last reads (the inverse
+        // transform's first exchange) are behind its second barrier, and
+        // after this transform's first barrier B is no longer read
+        fft_line_hook<T, N, E, false, true>(x, t, sA, 1, tw, [&] {
+          if (threadIdx.x == 0) prefetch(st ^ 1, q + gridDim.x);
+        });
+      } else {
+        fft_line<T, N, E, 1, false>(x, t, sB, 1, tw);
+      }
       C* dst = reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
       const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
 #pragma unroll
       for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
     } else {
+      if constexpr (DB) {
+        __syncthreads();  // B is no longer read
+        if (threadIdx.x == 0) prefetch(st ^ 1, q + gridDim.x);
+      }
       C* dst = reinterpret_cast<C*>(a.A) + slab + m * N + t;
 #pragma unroll
       for (int j = 0; j < E; ++j) dst[j * TPL] = x[j];
-    }
-    // the last exchange of the last transform used xch: every read of stage st
-    // is behind a barrier
-    if constexpr (DB) {
-      if (threadIdx.x == 0) refill(st, q);
     }
   }
 }
@@ -798,7 +827,7 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
     __syncthreads();  // every thread has read stage st
     C* sA = stage + st * SLW + c;
     if constexpr (DB) {
-      fft_line_db<T, N, E, 1, false, 0, true>(x, t, sA, xch + c, W, tw);
+      fft_line_db<T, N, E, 1, false, 0, 1>(x, t, sA, xch + c, W, tw);
     } else {
       if (threadIdx.x == 0) refill(st, i);
       fft_line<T, N, E, 1, false>(x, t, xch + c, W, tw);
@@ -811,7 +840,7 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
       for (int j = 0; j < E; ++j) x[j] = cmul<T>(x[j], mk<T>(T(pre[j].x), T(pre[j].y)));
     }
     if constexpr (DB) {
-      fft_line_db<T, N, E, 1, true, 0, true>(x, t, sA, xch + c, W, tw);
+      fft_line_db<T, N, E, 1, true, 0, 1>(x, t, sA, xch + c, W, tw);
       // the last exchange used xch, so every read of stage st is behind a barrier
       if (threadIdx.x == 0) refill(st, i);
     } else {
