@@ -31,6 +31,7 @@ SOURCES = [
     "rows_f64_c2.cu",
     "cols_f32.cu",
     "cols_f64.cu",
+    "fno.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -109,6 +109,28 @@ SIGNATURES = [
          ct.c_double, ct.c_void_p],
     ),
     ("nlse_square_mod", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_void_p]),
+] + [
+    # surrogate kernels (nlse_fno.h): p = pointer (device pointer or stream), l = int64,
+    # i = int32, f = float
+    (name, ct.c_int, [{"p": ct.c_void_p, "l": ct.c_int64, "i": ct.c_int32, "f": ct.c_float}[c]
+                      for c in sig])
+    for name, sig in [
+        ("nlse_fno_lift_rows", "lppppppp"),
+        ("nlse_fno_cols_analysis", "lpfippp"),
+        ("nlse_fno_mix", "lppppp"),
+        ("nlse_fno_cols_synthesis", "lppp"),
+        ("nlse_fno_layer_rows", "lppppipppppppp"),
+        ("nlse_fno_proj_bwd", "lpppppp"),
+        ("nlse_fno_layer_rows_bwd", "lpppippppppp"),
+        ("nlse_fno_lift_bwd", "lpppppp"),
+        ("nlse_fno_mix_wgrad", "lpppp"),
+        ("nlse_fno_reduce", "pllpp"),
+        ("nlse_fno_pack_spectral", "pppp"),
+        ("nlse_fno_pack_conv", "pppp"),
+        ("nlse_fno_loss", "lppppp"),
+        ("nlse_fno_adam", "pppplffffifp"),
+        ("nlse_fno_gemm_selftest", "pppiipp"),
+    ]
 ]
 
 _lock = threading.Lock()

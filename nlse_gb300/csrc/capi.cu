@@ -128,6 +128,14 @@ struct GraphKey {
 
 }  // namespace
 
+// Entry points shared with the other translation units of the library.
+namespace nlse {
+int shared_twiddles(int dev, int dtype, const void** out) { return get_twiddles(dev, dtype, out); }
+int shared_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+int shared_cuda_fail(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+void shared_clear_error() { g_err.clear(); }
+}  // namespace nlse
+
 struct nlse_plan_s {
   nlse_desc d;
   int dev = 0;

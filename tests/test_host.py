@@ -18,7 +18,7 @@ HEADER = ROOT / "include" / "nlse_gb300.h"
 
 
 def _declared_symbols():
-    text = HEADER.read_text()
+    text = "\n".join(h.read_text() for h in sorted(HEADER.parent.glob("*.h")))
     return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*|void)\s+(nlse_\w+)\(", text,
                                  re.M)))
 
