@@ -100,10 +100,11 @@ int nlse_fno_pack_spectral(const void* W, void* wf, void* wb, void* stream);
 /* BF16 operands of a 1 x 1 convolution wc [32][32] float (in x out). */
 int nlse_fno_pack_conv(const float* wc, void* wf, void* wb, void* stream);
 
-/* stats [nb][2] = (||out-tgt||^2, ||tgt||^2) per field; with dout != NULL the
- * gradient of mean_f ||out-tgt||^2 / ||tgt||^2 (complex64 [nb][256][256]). */
-int nlse_fno_loss(int64_t nb, const void* out, const void* tgt, float* stats, void* dout,
-                  void* stream);
+/* stats [nb][2] = (||out-tgt||^2, ||ref||^2) per field (ref = NULL: tgt); with
+ * dout != NULL the gradient of mean_f ||out-tgt||^2 / ||ref||^2 (complex64
+ * [nb][256][256]). */
+int nlse_fno_loss(int64_t nb, const void* out, const void* tgt, const void* ref, float* stats,
+                  void* dout, void* stream);
 
 /* Adam step (FP32) with decoupled weight decay wd. */
 int nlse_fno_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1,

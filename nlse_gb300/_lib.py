@@ -127,7 +127,7 @@ SIGNATURES = [
         ("nlse_fno_reduce", "pllpp"),
         ("nlse_fno_pack_spectral", "pppp"),
         ("nlse_fno_pack_conv", "pppp"),
-        ("nlse_fno_loss", "lppppp"),
+        ("nlse_fno_loss", "lpppppp"),
         ("nlse_fno_adam", "pppplffffifp"),
         ("nlse_fno_gemm_selftest", "pppiipp"),
     ]

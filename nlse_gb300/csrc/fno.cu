@@ -705,20 +705,22 @@ __global__ void k_pack_conv(const float* __restrict__ wc, __nv_bfloat16* __restr
 }
 
 // ---- loss and optimiser ----------------------------------------------------------
-// Per field b: stats[2b] = ||out - tgt||^2, stats[2b+1] = ||tgt||^2 (FP32 sums).
+// Per field b: stats[2b] = ||out - tgt||^2, stats[2b+1] = ||ref||^2 (FP32 sums).
 __global__ void __launch_bounds__(256) k_loss_stats(const float2* __restrict__ out,
                                                      const float2* __restrict__ tgt,
+                                                     const float2* __restrict__ ref,
                                                      float* __restrict__ stats) {
   __shared__ float red[2][8];
   const int64_t b = blockIdx.x;
   const float2* o = out + b * N * N;
   const float2* g = tgt + b * N * N;
+  const float2* q = ref + b * N * N;
   float e = 0.f, n = 0.f;
   for (int i = threadIdx.x; i < N * N; i += 256) {
-    const float2 u = o[i], v = g[i];
+    const float2 u = o[i], v = g[i], w = q[i];
     const float dx = u.x - v.x, dy = u.y - v.y;
     e = fmaf(dx, dx, fmaf(dy, dy, e));
-    n = fmaf(v.x, v.x, fmaf(v.y, v.y, n));
+    n = fmaf(w.x, w.x, fmaf(w.y, w.y, n));
   }
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) {
@@ -737,7 +739,7 @@ __global__ void __launch_bounds__(256) k_loss_stats(const float2* __restrict__ o
   }
 }
 
-// Loss = (1/nb) sum_b ||out_b - tgt_b||^2 / ||tgt_b||^2; dout = its gradient.
+// Loss = (1/nb) sum_b ||out_b - tgt_b||^2 / ||ref_b||^2; dout = its gradient.
 __global__ void k_loss_grad(const float2* __restrict__ out, const float2* __restrict__ tgt,
                             const float* __restrict__ stats, int64_t nb, float2* __restrict__ dout) {
   const int64_t total = nb * N * N;
@@ -1021,14 +1023,15 @@ int nlse_fno_pack_conv(const float* wc, void* wf, void* wb, void* stream) {
   return launched("nlse_fno_pack_conv");
 }
 
-int nlse_fno_loss(int64_t nb, const void* out, const void* tgt, float* stats, void* dout,
-                  void* stream) {
+int nlse_fno_loss(int64_t nb, const void* out, const void* tgt, const void* ref, float* stats,
+                  void* dout, void* stream) {
   nlse::shared_clear_error();
   if (bad_batch(nb) || !out || !tgt || !stats)
     return nlse::shared_fail(NLSE_ERR_ARG, "nlse_fno_loss: bad argument");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   k_loss_stats<<<(unsigned)nb, 256, 0, s>>>(reinterpret_cast<const float2*>(out),
-                                             reinterpret_cast<const float2*>(tgt), stats);
+                                             reinterpret_cast<const float2*>(tgt),
+                                             reinterpret_cast<const float2*>(ref ? ref : tgt), stats);
   if (dout)
     k_loss_grad<<<1024, 256, 0, s>>>(reinterpret_cast<const float2*>(out),
                                       reinterpret_cast<const float2*>(tgt), stats, nb,

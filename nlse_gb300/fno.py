@@ -100,7 +100,9 @@ class FNO:
         self.init(seed)
 
     # ---- parameters -----------------------------------------------------------
-    def init(self, seed: int = 0) -> None:
+    def init(self, seed: int = 0, out_scale: float = 1.0) -> None:
+        """Seeded initial weights; out_scale scales the projection (a small value
+        starts a residual predictor near zero)."""
         g = np.random.default_rng(seed)
         flat = np.zeros(self.size, np.float32)
         o = 0
@@ -108,8 +110,10 @@ class FNO:
             n = math.prod(s)
             if name == "wl":
                 flat[o:o + n] = g.normal(0, 1 / math.sqrt(5), n)
-            elif name.startswith("Wc") or name == "wp":
+            elif name.startswith("Wc"):
                 flat[o:o + n] = g.normal(0, 1 / math.sqrt(C), n)
+            elif name == "wp":
+                flat[o:o + n] = g.normal(0, out_scale / math.sqrt(C), n)
             elif name.startswith("W"):
                 flat[o:o + n] = g.normal(0, 1 / math.sqrt(2 * C), n)
             o += n
@@ -221,21 +225,24 @@ class FNO:
            "fno lift bwd")
         ck(L.nlse_fno_reduce(_ptr(ws.part), rows, PART_LIFT, _ptr(G["wl"]), s), "fno reduce")
 
-    def gradient(self, xin, xs, tgt) -> tuple[float, torch.Tensor]:
-        """Loss mean_b ||out_b - tgt_b||^2 / ||tgt_b||^2 and its gradient (flat, FP32)."""
+    def gradient(self, xin, xs, tgt, ref=None) -> tuple[float, torch.Tensor]:
+        """Loss mean_b ||out_b - tgt_b||^2 / ||ref_b||^2 (ref defaults to tgt) and its
+        gradient (flat, FP32)."""
         xin, xs = self._inputs(xin, xs, self.dev)
         tgt = torch.as_tensor(tgt).to(self.dev, torch.complex64).contiguous()
+        if ref is not None:
+            ref = torch.as_tensor(ref).to(self.dev, torch.complex64).contiguous()
         ws = self._workspace(xin.shape[0], True)
         out = self._forward(ws, xin, xs)
-        _lib.check(self.lib.nlse_fno_loss(ws.nb, _ptr(out), _ptr(tgt), _ptr(ws.stats),
+        _lib.check(self.lib.nlse_fno_loss(ws.nb, _ptr(out), _ptr(tgt), _ptr(ref), _ptr(ws.stats),
                                           _ptr(ws.dout), stream_handle(self.dev)), "fno loss")
         self._backward(ws, xin, xs)
         st = ws.stats
         loss = (st[:, 0] / st[:, 1].clamp_min(1e-30)).mean()
         return float(loss.item()), self.grad
 
-    def train_step(self, xin, xs, tgt, lr: float, wd: float = 0.0) -> float:
-        loss, _ = self.gradient(xin, xs, tgt)
+    def train_step(self, xin, xs, tgt, lr: float, wd: float = 0.0, ref=None) -> float:
+        loss, _ = self.gradient(xin, xs, tgt, ref)
         self.steps += 1
         _lib.check(self.lib.nlse_fno_adam(_ptr(self.flat), _ptr(self.grad), _ptr(self.m),
                                           _ptr(self.v), self.size, lr, 0.9, 0.999, 1e-8,

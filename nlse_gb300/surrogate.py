@@ -1,21 +1,28 @@
-"""Learned surrogate of the 256^2 NLSE propagation, with the solver as data
-source, fallback and judge.
+"""Learned surrogate of the 256^2 NLSE propagation, with the split-step solver
+as data source, fallback and judge.
 
 Workload: the 164-field configuration's distributions restricted to 256 x 256
 (power ~ U[0.1, 2] W, n2 = -10^U[-10, -8.4] m^2/W, Gaussian beam of waist
 ~ U[0.8, 2.5] mm, potential = sum of 1-8 Gaussian wells of depth
 U[0.5, 2]e-4 and width U[30, 150] um centred in the inner half-window;
 Isat = 1e5 W/m^2, alpha = 20 /m, L = 10 mm, dz = 5e-5 m, window 4 x 2.23 mm).
+The solver's output ("fine") is out_field(E0, L) with those parameters:
+count_steps(L, dz) = 201 Lie steps, i.e. a propagation length of 201 dz.
 
-The network (fno.FNO) maps (Re E0, Im E0, V) on the grid plus (power, n2)
-to E(L) / a, where a is the factor out_field's normalisation applies to E0;
-the prediction is a times the network output.
+Prediction (residual form): a coarse solve over the same length, `coarse`
+Strang steps, gives E_c; the network (fno.FNO) maps (Re E_c/a, Im E_c/a,
+V/1e-4) on the grid and the scalars (power, log10 |n2|) to the correction
+(E_fine - E_c) / (a * RES), where a is the factor out_field's power
+normalisation applies to E0.  Prediction: E_c + a * RES * net(...).  The
+nonlinear and potential phases of this workload reach tens of radians over L,
+which a 32-mode network does not map to 1e-2 from E0 alone; the correction to
+a coarse solve is small and smooth.  "Without the network" means E_c alone.
 
 Judge (the solver decides):
   * power check: the predicted field's power must lie within tol of
-    [P0 exp(-alpha L), P0].  Under the GPU path's saturated loss the power
-    decays more slowly than P0 exp(-alpha L), so that is a lower bound, and
-    the loss term cannot create power, so P0 is an upper bound;
+    [P0 exp(-alpha L'), P0] (L' the propagation length).  Under the GPU path's
+    saturated loss the power decays more slowly than P0 exp(-alpha L'), so
+    that is a lower bound, and the loss term cannot create power;
   * a seeded 1-in-`every` sample is re-solved; a sampled field whose
     prediction is off by more than tol (relative L2) takes the solver's
     field, and if more than `max_fail` of the sample fails, the whole batch
@@ -34,76 +41,91 @@ from scipy.constants import c, epsilon_0
 
 from . import engine
 from .fno import FNO
-from .nlse import NLSE
+from .nlse import NLSE, count_steps
 
 N = 256
 WINDOW, ALPHA, L, ISAT, DZ = 4 * 2.23e-3, 20.0, 10e-3, 1e5, 5e-5
 P_MID, P_HALF = 1.05, 0.95
 LOGN2_MID, LOGN2_HALF = -9.2, 0.8
 V_SCALE = 1e-4
+RES = 0.05  # scale of the learned correction relative to the field
+MAX_WELLS = 8
 
 
 def _grid():
     sim = NLSE(ALPHA, 1.0, WINDOW, -1e-9, None, L, NX=N, NY=N, Isat=ISAT)
-    return sim.XX, sim.YY, sim.delta_X, sim.delta_Y
+    return sim.X, sim.Y, sim.delta_X, sim.delta_Y
 
 
-def sample_inputs(n: int, seed: int = 0) -> dict:
-    """n seeded input sets: E0 (n, N, N) complex64 unit-peak beams, V (n, N, N)
-    float32, power (n,), n2 (n,)."""
+def fine_length() -> float:
+    """Propagation length of the solver's out_field(E0, L) loop (201 steps of dz)."""
+    return count_steps(L, DZ) * DZ
+
+
+def sample_inputs(n: int, seed: int = 0, device="cuda") -> dict:
+    """n seeded input sets: E0 (n, N, N) complex64 unit-peak beams and V (n, N, N)
+    float32 on the device; power (n,), n2 (n,) as host arrays."""
     rng = np.random.default_rng(seed)
-    XX, YY, _, _ = _grid()
     power = rng.uniform(0.1, 2.0, n)
     n2 = -(10.0 ** rng.uniform(-10, -8.4, n))
     waist = rng.uniform(0.8e-3, 2.5e-3, n)
-    V = np.zeros((n, N, N), np.float32)
-    E0 = np.empty((n, N, N), np.complex64)
-    r2 = XX**2 + YY**2
-    for b in range(n):
-        v = np.zeros((N, N))
-        for _ in range(rng.integers(1, 9)):
-            depth = rng.uniform(0.5e-4, 2e-4)
-            width = rng.uniform(30e-6, 150e-6)
-            x0, y0 = rng.uniform(-WINDOW / 4, WINDOW / 4, 2)
-            v -= depth * np.exp(-((XX - x0) ** 2 + (YY - y0) ** 2) / width**2)
-        V[b] = v
-        E0[b] = np.exp(-r2 / waist[b] ** 2)
-    return {"E0": E0, "V": V, "power": power, "n2": n2}
+    count = rng.integers(1, MAX_WELLS + 1, n)
+    depth = rng.uniform(0.5e-4, 2e-4, (n, MAX_WELLS)) * (np.arange(MAX_WELLS) < count[:, None])
+    width = rng.uniform(30e-6, 150e-6, (n, MAX_WELLS))
+    centre = rng.uniform(-WINDOW / 4, WINDOW / 4, (n, MAX_WELLS, 2))
+    X, Y, _, _ = _grid()
+    f64 = dict(dtype=torch.float64, device=device)
+    Xd, Yd = torch.as_tensor(X, **f64), torch.as_tensor(Y, **f64)
+    w = torch.as_tensor(width, **f64)[..., None]
+    gx = torch.exp(-(Xd - torch.as_tensor(centre[..., 0], **f64)[..., None]) ** 2 / w**2)
+    gy = torch.exp(-(Yd - torch.as_tensor(centre[..., 1], **f64)[..., None]) ** 2 / w**2)
+    V = -torch.einsum("bk,bki,bkj->bij", torch.as_tensor(depth, **f64), gy, gx)  # [y][x]
+    wb = torch.as_tensor(waist, **f64)[:, None]
+    E0 = torch.exp(-Yd**2 / wb**2)[:, :, None] * torch.exp(-Xd**2 / wb**2)[:, None, :]
+    return {"E0": E0.to(torch.complex64).contiguous(), "V": V.to(torch.float32).contiguous(),
+            "power": power, "n2": n2}
 
 
 def subset(inp: dict, idx) -> dict:
-    return {k: v[idx] for k, v in inp.items()}
+    """Input sets idx (a slice or an index array)."""
+    out = {}
+    for k, v in inp.items():
+        if isinstance(v, torch.Tensor) and not isinstance(idx, slice):
+            out[k] = v[torch.as_tensor(np.asarray(idx), device=v.device)]
+        else:
+            out[k] = v[idx]
+    return out
 
 
-def scale(inp: dict) -> np.ndarray:
-    """a per field: the factor out_field's power normalisation applies to E0."""
+def scale(inp: dict) -> torch.Tensor:
+    """a per field (device, float64): the factor out_field's power normalisation applies to E0."""
     _, _, dx, dy = _grid()
-    s = np.sum(np.abs(inp["E0"].astype(np.complex128)) ** 2, axis=(1, 2)) * dx * dy * c * epsilon_0 / 2
-    return np.sqrt(inp["power"] / s)
-
-
-def features(inp: dict) -> tuple[np.ndarray, np.ndarray]:
-    """Network inputs: xin (n, N, N, 3) = (Re E0, Im E0, V / 1e-4), xs (n, 2)."""
     E0 = inp["E0"]
-    xin = np.stack([E0.real, E0.imag, inp["V"] / V_SCALE], axis=-1).astype(np.float32)
-    xs = np.stack([(inp["power"] - P_MID) / P_HALF,
-                   (np.log10(-inp["n2"]) - LOGN2_MID) / LOGN2_HALF], axis=-1).astype(np.float32)
-    return xin, xs
+    s = engine.power(E0.contiguous(), E0.shape[0]) * (dx * dy * c * epsilon_0 / 2)
+    return torch.sqrt(torch.as_tensor(inp["power"], dtype=torch.float64, device=E0.device) / s)
 
 
-def solve(inp: dict, device="cuda", chunk: int = 2048) -> torch.Tensor:
-    """E(L) of every input set by the split-step solver, (n, N, N) complex64 on the device."""
-    n = len(inp["power"])
-    out = torch.empty((n, N, N), dtype=torch.complex64, device=device)
+def solve(inp: dict, steps: int | None = None, chunk: int = 2048) -> torch.Tensor:
+    """E at the solver's propagation length for every input set, (n, N, N)
+    complex64 on the device.  steps=None: the solver itself (out_field(E0, L),
+    Lie scheme, dz = 5e-5); otherwise `steps` Strang steps over the same length."""
+    E0all = inp["E0"]
+    n = E0all.shape[0]
+    out = torch.empty((n, N, N), dtype=torch.complex64, device=E0all.device)
     for b0 in range(0, n, chunk):
         sl = slice(b0, min(n, b0 + chunk))
         B = sl.stop - sl.start
         sim = NLSE(ALPHA, inp["power"][sl], WINDOW, inp["n2"][sl].reshape(B, 1, 1), None, L,
                    NX=N, NY=N, Isat=ISAT)
-        sim.delta_z = DZ
         sim.V = inp["V"][sl]
-        E0 = torch.from_numpy(np.ascontiguousarray(inp["E0"][sl])).to(device)
-        out[sl] = sim.out_field(E0, L, verbose=False)
+        if steps is None:
+            sim.delta_z = DZ
+            out[sl] = sim.out_field(E0all[sl], L, verbose=False)
+        else:
+            dz = fine_length() / steps
+            sim.delta_z = dz
+            out[sl] = sim.out_field(E0all[sl], (steps - 0.5) * dz, precision="double",
+                                    verbose=False)
     return out
 
 
@@ -122,24 +144,37 @@ def power(E: torch.Tensor) -> torch.Tensor:
 
 
 class Surrogate:
-    def __init__(self, device="cuda", seed: int = 0):
+    """Coarse Strang solve plus a learned correction, judged by the solver."""
+
+    def __init__(self, device="cuda", seed: int = 0, coarse: int = 4):
         self.dev = torch.device(device)
+        self.coarse = coarse
         self.net = FNO(self.dev, seed)
+        self.net.init(seed, out_scale=1e-2)
         self.history: list = []
 
-    def _prepare(self, inp: dict):
-        xin, xs = features(inp)
-        a = torch.as_tensor(scale(inp), dtype=torch.float32, device=self.dev)
-        return (torch.from_numpy(xin).to(self.dev), torch.from_numpy(xs).to(self.dev), a)
+    def features(self, inp: dict, Ec: torch.Tensor):
+        a = scale(inp).to(torch.float32)
+        e = Ec / a[:, None, None]
+        xin = torch.stack([e.real, e.imag, inp["V"] / V_SCALE], dim=-1).contiguous()
+        xs = torch.as_tensor(np.stack([(inp["power"] - P_MID) / P_HALF,
+                                       (np.log10(-inp["n2"]) - LOGN2_MID) / LOGN2_HALF], -1),
+                             dtype=torch.float32, device=self.dev)
+        return xin, xs, a
 
-    def fit(self, inp: dict, E_L: torch.Tensor, epochs: int = 10, batch: int = 32,
-            lr: float = 2e-3, time_budget: float | None = None, seed: int = 0) -> list:
-        """Adam on mean relative squared error of E(L)/a; cosine learning-rate decay."""
-        xin, xs, a = self._prepare(inp)
-        tgt = (E_L.to(self.dev) / a[:, None, None]).to(torch.complex64)
+    def fit(self, inp: dict, E_f: torch.Tensor, epochs: int = 10, batch: int = 32,
+            lr: float = 2e-3, time_budget: float | None = None, seed: int = 0,
+            E_c: torch.Tensor | None = None) -> list:
+        """Adam on mean_b ||pred_b - E_f,b||^2 / ||E_f,b||^2 (cosine learning-rate decay)."""
+        Ec = solve(inp, self.coarse) if E_c is None else E_c
+        xin, xs, a = self.features(inp, Ec)
+        sa = (a * RES)[:, None, None]
+        tgt = ((E_f - Ec) / sa).to(torch.complex64)
+        ref = (E_f / sa).to(torch.complex64)
         n = xin.shape[0]
         order = torch.from_numpy(np.random.default_rng(seed).permutation(n)).to(self.dev)
-        xin, xs, tgt = xin[order].contiguous(), xs[order].contiguous(), tgt[order].contiguous()
+        xin, xs = xin[order].contiguous(), xs[order].contiguous()
+        tgt, ref = tgt[order].contiguous(), ref[order].contiguous()
         steps_per_epoch = max(1, n // batch)
         total = epochs * steps_per_epoch
         t0 = time.perf_counter()
@@ -148,18 +183,21 @@ class Surrogate:
             shift = (ep * batch // 3) % max(1, n - batch + 1)
             for i in range(steps_per_epoch):
                 b0 = (shift + i * batch) % max(1, n - batch + 1)
+                sl = slice(b0, b0 + batch)
                 lr_t = lr * 0.5 * (1 + math.cos(math.pi * step / total))
-                loss = self.net.train_step(xin[b0:b0 + batch], xs[b0:b0 + batch],
-                                           tgt[b0:b0 + batch], lr_t)
-                self.history.append(loss)
+                self.history.append(self.net.train_step(xin[sl], xs[sl], tgt[sl], lr_t, ref=ref[sl]))
                 step += 1
                 if time_budget is not None and time.perf_counter() - t0 > time_budget:
                     return self.history
         return self.history
 
-    def predict(self, inp: dict) -> torch.Tensor:
-        xin, xs, a = self._prepare(inp)
-        return self.net.predict(xin, xs) * a[:, None, None]
+    def predict(self, inp: dict, E_c: torch.Tensor | None = None,
+                with_coarse: bool = False):
+        """Predicted E at the solver's propagation length (and optionally E_c)."""
+        Ec = solve(inp, self.coarse) if E_c is None else E_c
+        xin, xs, a = self.features(inp, Ec)
+        P = Ec + self.net.predict(xin, xs) * (a * RES)[:, None, None]
+        return (P, Ec) if with_coarse else P
 
     def judge(self, inp: dict, E_pred: torch.Tensor, every: int = 16, seed: int = 0,
               tol: float = 1e-2, max_fail: float = 0.25):
@@ -168,13 +206,13 @@ class Surrogate:
         out = E_pred.clone()
         P0 = torch.as_tensor(inp["power"], dtype=torch.float64, device=self.dev)
         Pp = power(out)
-        lo = P0 * math.exp(-ALPHA * L) * (1 - tol)
+        lo = P0 * math.exp(-ALPHA * fine_length()) * (1 - tol)
         bad_power = ((Pp < lo) | (Pp > P0 * (1 + tol))).cpu().numpy()
         rng = np.random.default_rng(seed)
         k = max(1, math.ceil(n / every))
         sample = np.sort(rng.choice(n, size=k, replace=False))
-        E_s = solve(subset(inp, sample), self.dev)
-        err = rel_l2(out[sample], E_s).cpu().numpy()
+        E_s = solve(subset(inp, sample))
+        err = rel_l2(out[torch.as_tensor(sample, device=self.dev)], E_s).cpu().numpy()
         fail = err > tol
         if fail.any():
             out[torch.as_tensor(sample[fail], device=self.dev)] = \
@@ -183,7 +221,7 @@ class Surrogate:
         redo = (np.setdiff1d(np.arange(n), sample) if whole
                 else np.setdiff1d(np.nonzero(bad_power)[0], sample))
         if redo.size:
-            out[torch.as_tensor(redo, device=self.dev)] = solve(subset(inp, redo), self.dev)
+            out[torch.as_tensor(redo, device=self.dev)] = solve(subset(inp, redo))
         report = {"fields": n, "sampled": int(k), "sample_rel_l2_median": float(np.median(err)),
                   "sample_rel_l2_max": float(err.max()), "sample_failed": int(fail.sum()),
                   "power_check_failed": int(bad_power.sum()), "batch_resolved": whole,
