@@ -49,6 +49,68 @@ B_ROW = 16 + 4   # inverse+forward row pass: read A, write A, read V
 B_COL = 16       # column pass: read A, write A (propagator L2-resident, shared by the batch)
 
 
+SUR_TRAIN, SUR_TEST, SUR_EPOCHS, SUR_COARSE, SUR_EVERY = 20480, 4096, 4, 5, 16
+
+
+def surrogate_leg(dev, n_train=SUR_TRAIN, n_test=SUR_TEST, epochs=SUR_EPOCHS):
+    """Surrogate vs solver on 256^2 fields (the 164-field distributions restricted to
+    256^2): train on solver pairs, then time, from device-resident inputs, the plain
+    batched solver and the surrogate (coarse Strang solve + network + judge with a
+    1-in-16 re-solved sample) on held-out fields."""
+    import torch
+
+    from nlse_gb300 import surrogate as sg
+
+    def T():
+        torch.cuda.synchronize()
+        return time.perf_counter()
+
+    t0 = T()
+    train = sg.sample_inputs(n_train, seed=21, device=dev)
+    Ef = sg.solve(train)
+    t1 = T()
+    Ec = sg.solve(train, SUR_COARSE)
+    s = sg.Surrogate(dev, seed=0, coarse=SUR_COARSE)
+    s.fit(train, Ef, epochs=epochs, batch=32, lr=2e-3, E_c=Ec)
+    t2 = T()
+    s.net.check_status()
+    del train, Ef, Ec
+    test = sg.sample_inputs(n_test, seed=22, device=dev)
+    warm = sg.subset(test, slice(0, 64))
+    sg.solve(warm)
+    s.judge(warm, s.predict(warm), every=SUR_EVERY)
+    ta = T()
+    ref = sg.solve(test)
+    tb = T()
+    P, Ec = s.predict(test, with_coarse=True)
+    tc = T()
+    out, rep = s.judge(test, P, every=SUR_EVERY, seed=23)
+    td = T()
+    xin, xs, _ = s.features(test, Ec)
+    tn0 = T()
+    s.net.predict(xin, xs)
+    tn1 = T()
+    q = [0.5, 0.9, 0.99, 1.0]
+    e_c, e_p, e_o = (sg.rel_l2(x, ref).cpu().numpy() for x in (Ec, P, out))
+
+    def stats(e):
+        return {"quantiles_50_90_99_max": [float(v) for v in np.quantile(e, q)],
+                "pass_1e-2": float((e <= 1e-2).mean())}
+
+    return {"workload": "256^2 c64 fields, 164-field distributions, L=10 mm (201 solver steps)",
+            "fields": n_test, "solver_fields_per_s": n_test / (tb - ta),
+            "surrogate_fields_per_s": n_test / (td - tb),
+            "surrogate_without_judge_fields_per_s": n_test / (tc - tb),
+            "network_only_fields_per_s": n_test / (tn1 - tn0),
+            "speedup_vs_solver": (tb - ta) / (td - tb),
+            "coarse_strang_steps": SUR_COARSE, "judge_sample": f"1 in {SUR_EVERY}",
+            "rel_l2_vs_solver": {"coarse_alone": stats(e_c), "coarse_plus_network": stats(e_p),
+                                 "after_judge": stats(e_o)},
+            "judge": rep,
+            "train": {"pairs": n_train, "epochs": epochs, "batch": 32, "data_s": t1 - t0,
+                      "train_s": t2 - t1, "final_loss": float(np.mean(s.history[-50:]))}}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -56,6 +118,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="leave out the surrogate-vs-solver leg (about a minute)")
     return ap.parse_args()
 
 
@@ -350,6 +414,9 @@ def run_gb300(args):
     mixed = {"fields": 164, "steps": nb, "field_steps_per_s": world * 164 * nb / tb,
              "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
                      "and potentials; one CUDA graph with a concurrent branch per grid size"}
+    sur = None
+    if rank == 0 and not args.no_surrogate:
+        sur = surrogate_leg(dev)
     if rank == 0:
         cb, _ = cpu_reference(4, 3, 1)
         cpu_base = cb
@@ -364,7 +431,8 @@ def run_gb300(args):
                            "fields_per_gpu": B, "grid": [N, N], "scheme": "single",
                            "l2": "inputs larger than L2 (256 MiB per GPU)",
                            "step_model_gbs_52B_per_pt": round(step_model_gbs, 1),
-                           "single_field_loop": single, "mixed_batch_164": mixed},
+                           "single_field_loop": single, "mixed_batch_164": mixed,
+                           "surrogate_256": sur},
                 "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line), flush=True)

@@ -79,7 +79,8 @@ def sample_inputs(n: int, seed: int = 0, device="cuda") -> dict:
     w = torch.as_tensor(width, **f64)[..., None]
     gx = torch.exp(-(Xd - torch.as_tensor(centre[..., 0], **f64)[..., None]) ** 2 / w**2)
     gy = torch.exp(-(Yd - torch.as_tensor(centre[..., 1], **f64)[..., None]) ** 2 / w**2)
-    V = -torch.einsum("bk,bki,bkj->bij", torch.as_tensor(depth, **f64), gy, gx)  # [y][x]
+    # V[y][x] = -sum_k depth_k gy_k(y) gx_k(x): one batched product of (N x wells) (wells x N)
+    V = -torch.bmm((gy * torch.as_tensor(depth, **f64)[..., None]).transpose(1, 2), gx)
     wb = torch.as_tensor(waist, **f64)[:, None]
     E0 = torch.exp(-Yd**2 / wb**2)[:, :, None] * torch.exp(-Xd**2 / wb**2)[:, None, :]
     return {"E0": E0.to(torch.complex64).contiguous(), "V": V.to(torch.float32).contiguous(),
