@@ -276,7 +276,11 @@ def run_gb300(args):
     sim.delta_z = DZ
     V = potential(sim.XX, sim.YY)
     sim.V = V
-    E_host = fields(sim.XX, sim.YY, B, 1000 + rank)
+    # weak scaling: the job is world x B whole fields; this rank owns one block
+    from nlse_gb300.shard import field_block
+
+    blk = field_block(world * B, rank, world)
+    E_host = fields(sim.XX, sim.YY, blk.stop - blk.start, 1000 + blk.start)
     A = torch.from_numpy(E_host).to(dev)
     sim.propagator = sim._build_propagator()
     plan = sim._build_fft_plan(A)[0]
