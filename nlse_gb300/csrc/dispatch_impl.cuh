@@ -23,7 +23,8 @@ static cudaError_t rows_tma_n(const StepArgs& a, cudaStream_t s, bool prep, bool
   if constexpr (OK_MODE && N >= 64 && (N / W) % ((N / W) < 256 ? (N / W) : 256) == 0 &&
                 rows_tma_smem<T, N, NC>() <= kMaxSmemPerCta) {
     constexpr int E = Shape<N>::E;
-    constexpr int THREADS = NC * (N / E);
+    constexpr int THREADS = RowTma<T, N, NC>::THREADS;
+    constexpr int LPC = RowTma<T, N, NC>::LPC;
     constexpr size_t smem = rows_tma_smem<T, N, NC>();
     auto kern = k_rows_tma<T, N, E, MODE, NC>;
     if (prep) {
@@ -39,8 +40,9 @@ static cudaError_t rows_tma_n(const StepArgs& a, cudaStream_t s, bool prep, bool
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
+    const int64_t groups = (a.nq + LPC - 1) / LPC;
     int64_t g = (int64_t)a.tma_grid * per_sm;
-    if (g > a.nq) g = a.nq;
+    if (g > groups) g = groups;
     kern<<<(unsigned)g, THREADS, smem, s>>>(a, *a.tmap);
     return cudaGetLastError();
   }
@@ -164,7 +166,14 @@ static cudaError_t cols_blk_tma_n(const ColArgs& a, cudaStream_t s, bool prep, i
       return set_smem(k_cols_blk_tma<T, N, E, false>, smem);
     }
     if (a.nblocks <= 0) return cudaSuccess;
-    const int64_t g = a.nblocks < grid ? a.nblocks : grid;
+    // persistent grid: every CTA that fits on the SMs (one per SM for long
+    // columns, several for short ones)
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int64_t g = (int64_t)grid * per_sm;
+    if (g > a.nblocks) g = a.nblocks;
     kern<<<(unsigned)g, THREADS, smem, s>>>(a);
     return cudaGetLastError();
   }

@@ -334,10 +334,11 @@ __device__ __forceinline__ void fft_line_db(cpx<T> (&x)[E], int t, cpx<T>* smA, 
 }
 
 // fft_line on one buffer whose first exchange needs no leading barrier (the
-// caller guarantees that no thread still reads sm), with hook() run by every
+// caller guarantees that no thread still reads sm, or passes LEAD), with hook() run by every
 // thread right after that exchange's barrier: at that point every read of
 // shared memory the caller issued before the transform has completed.
-template <typename T, int N, int E, bool INV, bool FENCE, typename Hook>
+// LEAD: start the first exchange with a barrier (when threads may still read sm).
+template <typename T, int N, int E, bool INV, bool FENCE, bool LEAD = false, typename Hook>
 __device__ __forceinline__ void fft_line_hook(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
                                               const cpx<T>* __restrict__ tw, Hook&& hook) {
   constexpr int R = PassRadix<N, E, 1>::R;
@@ -345,6 +346,7 @@ __device__ __forceinline__ void fft_line_hook(cpx<T> (&x)[E], int t, cpx<T>* sm,
   asm volatile("" : "+r"(t)::"memory");
   stockham_pass<T, N, E, R, 1, INV>(x, t, tw);
   if constexpr (R < N) {
+    if constexpr (LEAD) __syncthreads();
     exchange_store<T, N, E, 1>(x, t, sm, stride);
     if constexpr (FENCE) fence_async_after_stores();
     __syncthreads();

@@ -46,6 +46,8 @@ constexpr int WBIG = XK * XK;       // real 64 x 64 form of one mode's complex w
 constexpr int WCONV = C * C;
 constexpr int PS = 17;              // pair stride of the [pixel][channel pair] buffers
 constexpr float kSynFwd = 1.0f / (N * N);
+constexpr size_t kPairBuf =
+    (16 * SL > N * PS ? 16 * SL : N * PS) * sizeof(float2);  // shared by xl and the pairs
 
 __device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 __device__ __forceinline__ float gelu(float z) {
@@ -79,6 +81,11 @@ __device__ __forceinline__ void load_bf16x32(const __nv_bfloat16* src, float (&v
 }
 
 // ---- row transforms (one CTA of 256 threads per image row) ----------------
+// The exchange lines xl (16 x SL) and the pair buffer [pixel][channel pair]
+// (N x PS) are never live at once, so the kernels give both the same
+// storage (kPairBuf bytes): row_analysis reads its input before the first
+// exchange (whose leading barrier orders the reuse) and row_synthesis writes
+// its output after a barrier that follows the last exchange.
 // Forward half spectrum of one row of 32 real channels.  hs holds the row as
 // channel pairs, hs[x*PS + j] = (h_2j(x), h_2j+1(x)); line j is transformed as
 // z = h_2j + i h_2j+1 and split with H_2j = (Z(k) + conj Z(-k))/2,
@@ -131,6 +138,7 @@ __device__ void row_synthesis(const float2* __restrict__ U, float scale, float2*
     }
   }
   fft_line<float, N, E, 1, true>(x, t, xl + j * SL, 1, tw);
+  __syncthreads();  // ss may share storage with the exchange lines
 #pragma unroll
   for (int e = 0; e < E; ++e) ss[(t + TPL * e) * PS + j] = make_float2(scale * x[e].x, scale * x[e].y);
 }
@@ -145,7 +153,7 @@ __global__ void __launch_bounds__(256) k_lift_rows(const float* __restrict__ xin
                                                     float2* __restrict__ T, const float2* tw) {
   extern __shared__ __align__(128) unsigned char smraw[];
   float2* hs = reinterpret_cast<float2*>(smraw);
-  float2* xl = hs + N * PS;
+  float2* xl = hs;
   const int64_t row = blockIdx.x;
   const int64_t b = row / N;
   const int p = threadIdx.x;
@@ -330,8 +338,7 @@ struct LayerArgs {
   int* status;
 };
 
-constexpr size_t kLayerSmem = (size_t)16 * SL * sizeof(float2) + (size_t)N * PS * sizeof(float2) +
-                              (size_t)N * C * 2 + (size_t)WCONV * 2 + sizeof(TcState);
+constexpr size_t kLayerSmem = kPairBuf + (size_t)N * C * 2 + (size_t)WCONV * 2 + sizeof(TcState);
 
 __device__ __forceinline__ void stage_row_tiles(__nv_bfloat16* sA, const __nv_bfloat16* g) {
   // a 256 x 32 BF16 row block as two 128 x 32 canonical tiles
@@ -359,8 +366,8 @@ __device__ __forceinline__ void issue_row_conv(uint32_t tbase, const __nv_bfloat
 __global__ void __launch_bounds__(256) k_layer_rows(const LayerArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   float2* xl = reinterpret_cast<float2*>(smraw);
-  float2* ss = xl + 16 * SL;
-  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(ss + N * PS);
+  float2* ss = xl;
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smraw + kPairBuf);
   __nv_bfloat16* sW = sA + N * C;
   TcState* st = reinterpret_cast<TcState*>(sW + WCONV);
   const int64_t row = blockIdx.x;
@@ -464,8 +471,8 @@ constexpr size_t kBwdSmem = kLayerSmem + (size_t)N * (C + 1) * sizeof(float);
 __global__ void __launch_bounds__(256) k_layer_rows_bwd(const BwdArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   float2* xl = reinterpret_cast<float2*>(smraw);
-  float2* ss = xl + 16 * SL;
-  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(ss + N * PS);
+  float2* ss = xl;
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smraw + kPairBuf);
   __nv_bfloat16* sW = sA + N * C;
   TcState* st = reinterpret_cast<TcState*>(sW + WCONV);
   float* hsm = reinterpret_cast<float*>(st + 1);  // [N][C+1]
@@ -571,8 +578,8 @@ __global__ void __launch_bounds__(256) k_lift_bwd(const float* __restrict__ dhc_
                                                    float* __restrict__ part, const float2* tw) {
   extern __shared__ __align__(128) unsigned char smraw[];
   float2* xl = reinterpret_cast<float2*>(smraw);
-  float2* ss = xl + 16 * SL;
-  float* xsm = reinterpret_cast<float*>(ss + N * PS);  // [N][3]
+  float2* ss = xl;
+  float* xsm = reinterpret_cast<float*>(smraw + kPairBuf);  // [N][3]
   const int64_t row = blockIdx.x, b = row / N;
   const int p = threadIdx.x;
   const int64_t pix = row * N + p;
@@ -800,7 +807,7 @@ __global__ void __launch_bounds__(128) k_gemm_selftest(const __nv_bfloat16* __re
 }
 
 // ---- host side -------------------------------------------------------------------
-constexpr size_t kRowSmem = (size_t)N * PS * sizeof(float2) + (size_t)16 * SL * sizeof(float2);
+constexpr size_t kRowSmem = kPairBuf;
 constexpr size_t kLiftBwdSmem = kRowSmem + (size_t)N * 3 * sizeof(float);
 
 std::mutex g_attr_mu;

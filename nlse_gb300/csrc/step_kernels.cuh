@@ -509,69 +509,81 @@ __host__ __device__ constexpr int stage_len(int n) {
 
 constexpr int kRowStages = 2;
 
+// Shape of the TMA row pass: LPC lines (of NC components) per CTA, so that a
+// CTA has at least 128 threads when a line needs fewer.
+template <typename T, int N, int NC>
+struct RowTma {
+  static constexpr int E = Shape<N>::E, TPL = N / E;
+  static constexpr int LPC = (NC * TPL) >= 128 ? 1 : 128 / (NC * TPL);
+  static constexpr int THREADS = LPC * NC * TPL;
+  static constexpr int SLS = stage_len<T>(padded_len(N));
+};
+
 template <typename T, int N, int NC>
 __host__ __device__ constexpr size_t rows_tma_smem() {
-  // per component: two line buffers that alternate as staging and exchange
-  // buffers (an even number of exchanges per transform), else kRowStages
-  // staging lines and one exchange line; each padded
-  constexpr int nex = fft_exchanges(N, Shape<N>::E);
-  constexpr int nbuf = (nex > 0 && nex % 2 == 0) ? 2 : kRowStages + 1;
-  return (size_t)nbuf * NC * stage_len<T>(padded_len(N)) * sizeof(cpx<T>) +
+  // two buffers of LPC x NC padded lines that alternate as staging and
+  // exchange buffers, and one mbarrier per buffer
+  return (size_t)2 * RowTma<T, N, NC>::LPC * NC * RowTma<T, N, NC>::SLS * sizeof(cpx<T>) +
          kRowStages * sizeof(uint64_t);
 }
 
 template <typename T, int N, int E, int MODE, int NC>
-__global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
-                                                          const __grid_constant__ CUtensorMap tmS) {
+__global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
+    const StepArgs a, const __grid_constant__ CUtensorMap tmS) {
   using C = cpx<T>;
-  constexpr int TPL = N / E, W = BlkW<T>::W, NB = N / W;
+  using RT = RowTma<T, N, NC>;
+  constexpr int TPL = N / E, W = BlkW<T>::W, NB = N / W, LPC = RT::LPC, SLS = RT::SLS;
   constexpr int BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
   constexpr unsigned ROW_BYTES = N * sizeof(C);
-  constexpr int SL = padded_len(N);
   constexpr bool two = NC == 2;
-  static_assert(E == Shape<N>::E, "shared-memory size assumes Shape<N>::E");
-  // DB (an even number of exchanges per transform): two buffers X0, X1 of NC
-  // lines.  Line i arrives in X[i&1] by a tensor-map copy; its transforms use
-  // X[i&1] (A) and X[(i+1)&1] (B) as exchange buffers, the forward transform
-  // only A, and B receives line i+1 as soon as the forward transform's first
-  // barrier has passed.  Otherwise: a two-stage staging ring X0, X1, refilled
-  // as soon as read, and the exchange buffer X2.
-  constexpr int NEX = fft_exchanges(N, E);
-  constexpr bool DB = NEX > 0 && NEX % 2 == 0;
-  constexpr int NBUF = DB ? 2 : kRowStages + 1;
-  extern __shared__ __align__(128) unsigned char smraw[];
-  constexpr int SLS = stage_len<T>(SL);  // stride of the line buffers
+  static_assert(E == RT::E, "shared-memory size assumes Shape<N>::E");
   static_assert((SLS * sizeof(C)) % 128 == 0 && (BOXB * W * sizeof(C)) % 128 == 0,
                 "tensor-map copies need 128-byte aligned shared destinations");
+  // A CTA takes a group of LPC consecutive lines per iteration.  Two buffers
+  // X0, X1 (LPC x NC padded lines each) alternate: group i arrives in X[i&1]
+  // by tensor-map copies; its inverse transform uses X[i&1] (A) and, with two
+  // exchanges, X[(i+1)&1] (B); the forward transform uses A alone, and B
+  // receives group i+1 as soon as the forward transform's first barrier has
+  // passed.  With a single exchange per transform the forward transform
+  // starts with a barrier (A was just read by the inverse one).
+  constexpr int NEX = fft_exchanges(N, E);
+  static_assert(NEX == 1 || NEX == 2, "one or two exchanges per transform");
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(X + NBUF * NC * SLS);
-  auto buf = [&](int b, int cc) { return X + (b * NC + cc) * SLS; };
+  uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * NC * SLS);
+  auto buf = [&](int b, int li, int cc) { return X + ((b * LPC + li) * NC + cc) * SLS; };
   const C* tw = reinterpret_cast<const C*>(a.tw);
-  const int comp = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  const int li = threadIdx.x / (NC * TPL);
+  const int comp = (threadIdx.x / TPL) % NC, t = threadIdx.x % TPL;
   // line indices fit 32 bits (checked when the kernel is chosen), so the
   // per-line division below is a 32-bit one
   const unsigned nq = (unsigned)a.nq;
+  const unsigned ngroups = (nq + LPC - 1) / LPC;
 
-  // pixel-line q = (line y, field f) with the field fastest: CTAs of one wave
-  // take the same line of all fields and share its potential values in L2
+  // pixel-line q = (line y, field f) with the field fastest: the lines of a
+  // group and the CTAs of a wave share potential lines in L2
   const unsigned nf = nq / (unsigned)a.lines_per_comp;
   auto q_f = [&](unsigned q) { return q % nf; };
   auto q_y = [&](unsigned q) { return q / nf; };
-  auto issue = [&](int b, unsigned q) {
-    const unsigned f = q_f(q), y = q_y(q);
-    mbar_arrive_expect_tx(&bar[b], NC * ROW_BYTES);
+  auto issue = [&](int b, unsigned g) {
+    const unsigned q0 = g * LPC;
+    const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+    mbar_arrive_expect_tx(&bar[b], nl * NC * ROW_BYTES);
+    for (unsigned l = 0; l < nl; ++l) {
+      const unsigned f = q_f(q0 + l), y = q_y(q0 + l);
 #pragma unroll
-    for (int cc = 0; cc < NC; ++cc)
+      for (int cc = 0; cc < NC; ++cc)
 #pragma unroll
-      for (int bx = 0; bx < NBOX; ++bx)
-        tensor_load_4d(buf(b, cc) + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
-                       (int)(f * NC + cc), &bar[b]);
+        for (int bx = 0; bx < NBOX; ++bx)
+          tensor_load_4d(buf(b, (int)l, cc) + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB,
+                         (int)(f * NC + cc), &bar[b]);
+    }
   };
-  // load line qn into buffer b once every generic access to b is complete
-  auto prefetch = [&](int b, unsigned qn) {
-    if (qn < nq) {
+  // load group gn into buffer b once every generic access to b is complete
+  auto prefetch = [&](int b, unsigned gn) {
+    if (gn < ngroups) {
       fence_proxy_async_smem();
-      issue(b, qn);
+      issue(b, gn);
     }
   };
 
@@ -580,31 +592,28 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
     mbar_init_fence();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    constexpr int first = DB ? 1 : kRowStages;
-    for (int st = 0; st < first; ++st) {
-      const unsigned q = blockIdx.x + (unsigned)st * gridDim.x;
-      if (q < nq) issue(st, q);
-    }
-  }
+  if (threadIdx.x == 0 && blockIdx.x < ngroups) issue(0, blockIdx.x);
   int it = 0;
-  for (unsigned q = blockIdx.x; q < nq; q += gridDim.x, ++it) {
+  for (unsigned g = blockIdx.x; g < ngroups; g += gridDim.x, ++it) {
     const int st = it & 1;  // kRowStages == 2
     const unsigned par = (it >> 1) & 1;
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
-      // give up: record it, let the copies in flight land (bounded), leave
+      // give up: record it, let the copy in flight land (bounded), leave
       if (threadIdx.x == 0) {
         atomicExch(a.status, DEV_WAIT_TIMEOUT);
         mbar_wait_bounded(&bar[st], par);
-        if (!DB && q + gridDim.x < nq) mbar_wait_bounded(&bar[st ^ 1], ((it + 1) >> 1) & 1);
       }
       return;
     }
-    const int64_t f = q_f(q), m = q_y(q);
+    // lines past the end (last group) compute on an in-range line and store nothing
+    const unsigned q = g * LPC + li;
+    const bool act = q < nq;
+    const unsigned qc = act ? q : nq - 1;
+    const int64_t f = q_f(qc), m = q_y(qc);
     const int64_t pix0 = m * (int64_t)N + t;
     C x[E], xo[E];
-    C* sA = buf(st, comp);
+    C* sA = buf(st, li, comp);
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sA[t + j * TPL];
     VPre<E> vpre;
@@ -615,22 +624,16 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       for (int j = 0; j < E; ++j) vpre.v[j] = __ldg(vp + j * TPL);
     }
     __syncthreads();  // every thread has read its line from buffer st
-    const int bB = DB ? (st ^ 1) : kRowStages;
-    C* sB = buf(bB, comp);   // second exchange buffer
-    C* xpart = buf(bB, 0);   // partner exchange region (NC lines)
-    if constexpr (DB) {
-      fft_line_db<T, N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
-    } else {
-      if (threadIdx.x == 0) prefetch(st, q + (unsigned)kRowStages * gridDim.x);
-      fft_line<T, N, E, 1, true>(x, t, sB, 1, tw);
-    }
+    C* sB = buf(st ^ 1, li, comp);  // second exchange buffer
+    C* xpart = buf(st ^ 1, li, 0);  // partner exchange region (NC lines)
+    fft_line_db<T, N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
     const T sc = inv_n_of<T>(a);
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], sc);
     if (!(a.flags & F_NO_POST)) {
       if (two) {
         exchange_partner<T, N, E>(x, xo, xpart, comp, t);
-        if (DB) fence_proxy_async_smem();
+        fence_proxy_async_smem();
       }
       nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 0, true, &vpre);
     }
@@ -639,32 +642,29 @@ __global__ void __launch_bounds__(NC*(N / E)) k_rows_tma(const StepArgs a,
       if (a.flags & F_PRE_NL) {
         if (two) {
           exchange_partner<T, N, E>(x, xo, xpart, comp, t);
-          if (DB) fence_proxy_async_smem();
+          fence_proxy_async_smem();
         }
         nl_line<T, E, TPL, NC>(x, xo, a, f, comp, pix0, 1, false);
       }
-      if constexpr (DB) {
-        // forward transform in A alone: A's last reads (the inverse
-        // transform's first exchange) are behind its second barrier, and
-        // after this transform's first barrier B is no longer read
-        fft_line_hook<T, N, E, false, true>(x, t, sA, 1, tw, [&] {
-          if (threadIdx.x == 0) prefetch(st ^ 1, q + gridDim.x);
-        });
-      } else {
-        fft_line<T, N, E, 1, false>(x, t, sB, 1, tw);
-      }
-      C* dst = reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
-      const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
+      // forward transform in A alone; after its first barrier B is no longer read
+      fft_line_hook<T, N, E, false, true, NEX == 1>(x, t, sA, 1, tw, [&] {
+        if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
+      });
+      if (act) {
+        C* dst =
+            reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
+        const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
 #pragma unroll
-      for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
+        for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
+      }
     } else {
-      if constexpr (DB) {
-        __syncthreads();  // B is no longer read
-        if (threadIdx.x == 0) prefetch(st ^ 1, q + gridDim.x);
-      }
-      C* dst = reinterpret_cast<C*>(a.A) + slab + m * N + t;
+      __syncthreads();  // B is no longer read
+      if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
+      if (act) {
+        C* dst = reinterpret_cast<C*>(a.A) + slab + m * N + t;
 #pragma unroll
-      for (int j = 0; j < E; ++j) dst[j * TPL] = x[j];
+        for (int j = 0; j < E; ++j) dst[j * TPL] = x[j];
+      }
     }
   }
 }

@@ -215,30 +215,32 @@ class NLSE:
     _DEVICE_ATTRS = ("power", "n2", "alpha", "I_sat")
 
     def _send_arrays_to_gpu(self) -> None:
-        """Move the potential, propagator and array parameters to the device (nlse.py:309-342)."""
+        """Move the potential, propagator and array parameters to the device (nlse.py:309-342).
+
+        Records which of them were host arrays: only those go back to the host
+        afterwards (device tensors a caller supplied stay where they are)."""
         dev = self._device
-        if self.V is not None:
-            self.V = engine.to_device(self.V, dev)
-        self.nl_profile = engine.to_device(self.nl_profile, dev)
-        if self.propagator is not None:
-            self.propagator = engine.to_device(self.propagator, dev)
+        host = set()
+        for name in ("V", "nl_profile", "propagator"):
+            v = getattr(self, name, None)
+            if v is not None:
+                if not _is_device_array(v):
+                    host.add(name)
+                setattr(self, name, engine.to_device(v, dev))
         for name in self._DEVICE_ATTRS:
             v = getattr(self, name, None)
             if isinstance(v, np.ndarray):
+                host.add(name)
                 setattr(self, name, engine.to_device(v, dev))
+        self._host_attrs = host
 
     def _retrieve_arrays_from_gpu(self) -> None:
-        """Bring the device arrays back to NumPy (nlse.py:344-370)."""
-        if self.V is not None and _is_device_array(self.V):
-            self.V = self.V.cpu().numpy()
-        if _is_device_array(self.nl_profile):
-            self.nl_profile = self.nl_profile.cpu().numpy()
-        if _is_device_array(self.propagator):
-            self.propagator = self.propagator.cpu().numpy()
-        for name in self._DEVICE_ATTRS:
+        """Bring the arrays that were host arrays back to NumPy (nlse.py:344-370)."""
+        for name in getattr(self, "_host_attrs", ()):
             v = getattr(self, name, None)
             if _is_device_array(v):
                 setattr(self, name, v.cpu().numpy())
+        self._host_attrs = set()
 
     # -- the split-step operator --------------------------------------------
     def _nl_block(self, lead: tuple, precision: str, has_v: bool) -> np.ndarray:
