@@ -286,6 +286,10 @@ def run_gb300(args):
     plan = sim._build_fft_plan(A)[0]
     op = sim._operator(A, torch.from_numpy(V).to(dev), sim.propagator, "single")
 
+    # kernel variants picked by the autotuner (cached per GPU and geometry)
+    from nlse_gb300 import autotune
+
+    tuned = autotune.tune(plan, A.clone(), op)
     # warm-up (also captures and instantiates the graph)
     engine.propagate(plan, A, op, args.warmup, 0, graph=True)
     torch.cuda.synchronize()
@@ -435,6 +439,7 @@ def run_gb300(args):
                            "fields_per_gpu": B, "grid": [N, N], "scheme": "single",
                            "l2": "inputs larger than L2 (256 MiB per GPU)",
                            "step_model_gbs_52B_per_pt": round(step_model_gbs, 1),
+                           "kernel_variant": tuned,
                            "single_field_loop": single, "mixed_batch_164": mixed,
                            "surrogate_256": sur},
                 "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,

@@ -150,6 +150,17 @@ int nlse_group_propagate(nlse_group group, int32_t ngroups, const nlse_plan* pla
                          void* const* fields, const nlse_operator* ops, const int64_t* nsteps,
                          void* stream);
 
+/* Kernel variants of a plan's 2-D passes: TMA-fed persistent row passes
+ * (rows_tma) or one CTA per line, TMA-fed persistent column passes (cols_tma)
+ * or one CTA per tile.  The arithmetic is the same either way (results agree
+ * to rounding: the kernels fuse multiply-adds differently); the choice is a
+ * speed one (nlse_gb300.autotune times them).  No reference counterpart (the
+ * reference's VkFFTApp(tune=True) tunes its FFT plan, NLSE/nlse.py:216).
+ * Returns NLSE_ERR_UNSUPPORTED for a variant the plan does not have. */
+int nlse_plan_set_kernels(nlse_plan plan, int32_t rows_tma, int32_t cols_tma);
+int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
+                          int32_t* rows_tma_ok, int32_t* cols_tma_ok);
+
 /*
  * Nonlocal response (the reference's oaconvolve(|A|^2, nl_profile, "same")
  * over the transform axes, NLSE/nlse.py:143-155, 406-408, 444-447 and the

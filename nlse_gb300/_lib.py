@@ -65,6 +65,8 @@ SIGNATURES = [
     ("nlse_plan_destroy", ct.c_int, [ct.c_void_p]),
     ("nlse_plan_status", ct.c_int, [ct.c_void_p, ct.c_void_p]),
     ("nlse_plan_set_nonlocal", ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int64]),
+    ("nlse_plan_set_kernels", ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32]),
+    ("nlse_plan_get_kernels", ct.c_int, [ct.c_void_p] + [ct.POINTER(ct.c_int32)] * 4),
     ("nlse_group_create", ct.c_int, [ct.POINTER(ct.c_void_p)]),
     ("nlse_group_destroy", ct.c_int, [ct.c_void_p]),
     (

@@ -15,7 +15,7 @@ import ctypes as ct
 import numpy as np
 import torch
 
-from . import _lib, engine
+from . import _lib, autotune, engine
 from .engine import Plan
 from .nlse import count_steps
 
@@ -76,6 +76,8 @@ def out_fields(jobs, z: float, precision: str = "single", normalize: bool = True
             if z > simu.L:
                 simu.n2 = 0
             op = simu._operator(A, V, simu.propagator, precision, None, plan)
+            # the same kernel variant as out_field on this geometry (shared tuning cache)
+            autotune.maybe_tune(plan, A, op)
             prepared.append((simu, E_in, A, plan, op, count_steps(z, simu.delta_z), n2_old))
         n = len(prepared)
         plans = (ct.c_void_p * n)(*[p[3].handle.value for p in prepared])

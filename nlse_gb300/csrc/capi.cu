@@ -120,8 +120,9 @@ struct GraphKey {
   void* A;
   nlse_operator op;
   int64_t nsteps, step0;
+  uint64_t kgen;
   bool operator==(const GraphKey& o) const {
-    return A == o.A && nsteps == o.nsteps && step0 == o.step0 &&
+    return A == o.A && nsteps == o.nsteps && step0 == o.step0 && kgen == o.kgen &&
            std::memcmp(&op, &o.op, sizeof(op)) == 0;
   }
 };
@@ -160,7 +161,10 @@ struct nlse_plan_s {
   int* status = nullptr;        // device status word: DEV_* codes from bounded waits
   int nsm = 0;                  // multiprocessors (persistent grids)
   bool cols_tma = true;         // use the TMA-ring column pass where it fits
-  bool rows_tma = false;        // tensor map of S encoded: TMA-fed inverse row passes
+  bool rows_tma = false;        // use the TMA-fed inverse row passes
+  bool cols_tma_ok = true;      // the TMA column pass is available (not disabled)
+  bool rows_tma_ok = false;     // tensor map of S encoded: the TMA row passes are available
+  uint64_t kgen = 0;            // kernel-variant generation (part of every graph key)
   CUtensorMap tmS;              // S as {2W scalars, NY, NX/W, slabs}, box = one row (<= 256 runs)
   // nonlocal response: zero-padded grid (py x px), its scratch and FFT plan
   int64_t nl_py = 0, nl_px = 0;
@@ -630,7 +634,7 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, p->dev);
     if (e != cudaSuccess) rc = cuda_fail(e, "plan buffers");
     const char* env = getenv("NLSE_COLS_TMA");
-    if (env && env[0] == '0') p->cols_tma = false;
+    if (env && env[0] == '0') p->cols_tma = p->cols_tma_ok = false;
   }
   if (rc == NLSE_OK && p->blk) {
     const size_t es = d.dtype == NLSE_C64 ? 8 : 16;
@@ -641,7 +645,7 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     const bool want = !(env && env[0] == '0');
     const int64_t nb = d.shape[1] / blk_width(p);
     if (rc == NLSE_OK && want && (nb <= 256 || nb % 256 == 0) && d.nfields * d.comps < (1ll << 31))
-      p->rows_tma = encode_tmap_S(&p->tmS, p->S, d, p->pix);
+      p->rows_tma = p->rows_tma_ok = encode_tmap_S(&p->tmS, p->S, d, p->pix);
   }
   if (rc == NLSE_OK && p->fft_ok) rc = prepare_kernels(p);
   if (rc == NLSE_OK) {
@@ -731,6 +735,7 @@ int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* 
   put(fields, sizeof(void*) * n);
   put(ops, sizeof(nlse_operator) * n);
   put(nsteps, sizeof(int64_t) * n);
+  for (int i = 0; i < n; ++i) put(&plans[i]->kgen, sizeof(uint64_t));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (!(g->gexec && key == g->key)) {
     while ((int)g->branch.size() < n) {
@@ -802,7 +807,7 @@ int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (!(flags & NLSE_RUN_GRAPH)) return enqueue_steps(p, A, op, nsteps, step0, s);
 
-  GraphKey key{A, *op, nsteps, step0};
+  GraphKey key{A, *op, nsteps, step0, p->kgen};
   if (!(p->gvalid && p->gkey == key)) {
     // Capture on the plan's private stream, ordered after the caller's work
     // only at launch time (the graph itself has no external dependencies).
@@ -853,6 +858,33 @@ int nlse_pass(nlse_plan p, void* A, const nlse_operator* op, int32_t pass, int64
   int rc = check_op(p, op);
   if (rc != NLSE_OK) return rc;
   return enqueue_pass(p, A, op, pass, step, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nlse_plan_set_kernels(nlse_plan p, int32_t rows_tma, int32_t cols_tma) {
+  g_err.clear();
+  if (!p) return fail(NLSE_ERR_ARG, "null plan");
+  if (rows_tma && !p->rows_tma_ok)
+    return fail(NLSE_ERR_UNSUPPORTED, "this plan has no TMA row pass (geometry or disabled)");
+  if (cols_tma && !p->cols_tma_ok)
+    return fail(NLSE_ERR_UNSUPPORTED, "the TMA column pass is disabled for this plan");
+  if (p->rows_tma != (rows_tma != 0) || p->cols_tma != (cols_tma != 0)) {
+    p->rows_tma = rows_tma != 0;
+    p->cols_tma = cols_tma != 0;
+    ++p->kgen;  // captured graphs hold the old kernels
+  }
+  return NLSE_OK;
+}
+
+int nlse_plan_get_kernels(nlse_plan p, int32_t* rows_tma, int32_t* cols_tma,
+                          int32_t* rows_tma_ok, int32_t* cols_tma_ok) {
+  g_err.clear();
+  if (!p || !rows_tma || !cols_tma || !rows_tma_ok || !cols_tma_ok)
+    return fail(NLSE_ERR_ARG, "null argument");
+  *rows_tma = p->rows_tma;
+  *cols_tma = p->cols_tma;
+  *rows_tma_ok = p->rows_tma_ok;
+  *cols_tma_ok = p->cols_tma_ok;
+  return NLSE_OK;
 }
 
 int nlse_plan_set_nonlocal(nlse_plan p, int64_t pad_y, int64_t pad_x) {

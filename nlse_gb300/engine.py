@@ -89,6 +89,18 @@ class Plan:
             _lib.check(self.lib.nlse_plan_set_nonlocal(self.handle, py, px), "nonlocal grid")
         self._nl_pads = pads
 
+    def set_kernels(self, rows_tma: bool, cols_tma: bool) -> None:
+        """Choose the 2-D passes' kernel variants (nlse_plan_set_kernels)."""
+        _lib.check(self.lib.nlse_plan_set_kernels(self.handle, int(rows_tma), int(cols_tma)),
+                   "kernel variant")
+
+    def get_kernels(self) -> tuple:
+        """(rows_tma, cols_tma, rows_tma available, cols_tma available)."""
+        v = [ct.c_int32() for _ in range(4)]
+        _lib.check(self.lib.nlse_plan_get_kernels(self.handle, *[ct.byref(x) for x in v]),
+                   "kernel variant")
+        return tuple(bool(x.value) for x in v)
+
     def status(self) -> None:
         """Synchronise and raise if a kernel of this plan gave up a bounded wait."""
         with torch.cuda.device(self.device):

@@ -17,7 +17,7 @@ import torch
 from scipy import special
 from scipy.constants import c, epsilon_0
 
-from . import engine
+from . import autotune, engine
 from .engine import OperatorData, Plan
 
 __BACKEND__ = "GPU"
@@ -391,6 +391,7 @@ class NLSE:
                                      f"runs {n} steps")
                 if n > 0:
                     op = self._operator(A, V, self.propagator, precision, pump, self.plans[0])
+                    autotune.maybe_tune(self.plans[0], A, op)
                     engine.propagate(self.plans[0], A, op, n, 0, graph=True)
             else:
                 z_prop = 0
