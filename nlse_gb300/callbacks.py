@@ -64,3 +64,71 @@ def adapt_delta_z(simu, A, z: float, i: int, update_every: int, delta_z: list) -
         delta_n = n2 * A_sq / (1 + A_sq / simu.I_sat)
         z_nl = float(1 / (simu.k * float(delta_n.max())))
         simu.delta_z = np.abs(z_nl) / 12
+
+
+# ---- callbacks as graph nodes ------------------------------------------------
+# norm and sample read only the live field, so when every callback of a loop
+# is one of them the whole z-loop becomes one CUDA graph: segments of steps up
+# to each recording step, then the recording nodes (an FP64 power sum or a
+# device copy into a preallocated slot).  Results reach the caller's arrays
+# once, after the loop.  No per-step host synchronisation.
+
+_DEVICE_KINDS = {}
+
+
+def device_plan(callback, callback_args):
+    """[(kind, save_every, destination)] if every callback can run as graph
+    nodes, else None (NLSE_DEVICE_CALLBACKS=0 turns this off)."""
+    import os
+
+    if os.environ.get("NLSE_DEVICE_CALLBACKS", "") == "0":
+        return None
+    if not _DEVICE_KINDS:
+        _DEVICE_KINDS.update({norm: "norm", sample: "sample"})
+    if callable(callback):
+        pairs = [(callback, callback_args)]
+    elif isinstance(callback, list) and callback and all(callable(cb) for cb in callback):
+        pairs = list(zip(callback, callback_args))
+    else:
+        return None
+    out = []
+    for cb, args in pairs:
+        kind = _DEVICE_KINDS.get(cb)
+        if kind is None or len(args) != 2 or int(args[0]) <= 0:
+            return None
+        out.append((kind, int(args[0]), args[1]))
+    return out
+
+
+def run_in_graph(plan, A: torch.Tensor, op, n: int, recs) -> bool:
+    """Advance A by n steps with the recordings of recs as graph nodes; False
+    (nothing done) if the recording buffers would not fit comfortably."""
+    counts = [len(range(0, n, s)) for _, s, _ in recs]
+    need = sum(c * (A.numel() * A.element_size() if k == "sample" else 8)
+               for (k, _, _), c in zip(recs, counts))
+    free, _ = torch.cuda.mem_get_info(A.device)
+    if need > free // 4:
+        return False
+    bufs = [torch.empty((c,) + (tuple(A.shape) if k == "sample" else ()),
+                        dtype=A.dtype if k == "sample" else torch.float64, device=A.device)
+            for (k, _, _), c in zip(recs, counts)]
+    points = sorted({i for _, s, _ in recs for i in range(0, n, s)})
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        i0 = 0
+        for p in points:
+            engine.propagate(plan, A, op, p + 1 - i0, i0, graph=False)
+            i0 = p + 1
+            for (kind, s, _), buf in zip(recs, bufs):
+                if p % s == 0:
+                    if kind == "norm":
+                        buf[p // s].copy_(engine.power(A, 1)[0])
+                    else:
+                        buf[p // s].copy_(A)
+        if i0 < n:
+            engine.propagate(plan, A, op, n - i0, i0, graph=False)
+    g.replay()
+    for (kind, _, dst), buf in zip(recs, bufs):
+        for j in range(buf.shape[0]):
+            _store(dst, j, buf[j] if kind == "sample" else buf[j])
+    return True

@@ -17,7 +17,7 @@ import torch
 from scipy import special
 from scipy.constants import c, epsilon_0
 
-from . import autotune, engine
+from . import autotune, callbacks, engine
 from .engine import OperatorData, Plan
 
 __BACKEND__ = "GPU"
@@ -356,8 +356,10 @@ class NLSE:
         """Propagate the field over a distance z (nlse.py:489-619).
 
         Without callbacks the whole z-loop is one nlse_propagate call replayed
-        from a CUDA graph; with callbacks each step is one call followed by the
-        callbacks on the live device field, as in the reference loop.
+        from a CUDA graph; with only the norm / sample callbacks the loop and
+        their recordings are one graph (results copied out at the end); with
+        other callbacks each step is one call followed by the callbacks on the
+        live device field, as in the reference loop.
         Returns the field in proper units (V/m): a NumPy array for NumPy input,
         a torch tensor for torch input.
         """
@@ -384,7 +386,21 @@ class NLSE:
             if z > self.L:
                 self.n2 = 0
             plen = None if pump is None else min(pump[1].numel(), pump[3].numel())
-            if callback is None:
+            recs = None if callback is None or pump is not None else callbacks.device_plan(
+                callback, callback_args)
+            if recs is not None:
+                # norm / sample callbacks as nodes of one graph over the whole loop
+                n = count_steps(z, self.delta_z)
+                done = n == 0
+                if n > 0:
+                    op = self._operator(A, V, self.propagator, precision, None, self.plans[0])
+                    autotune.maybe_tune(self.plans[0], A, op)
+                    done = callbacks.run_in_graph(self.plans[0], A, op, n, recs)
+                if done:
+                    callback = None
+            if callback is None and recs is not None:
+                pass  # ran above
+            elif callback is None:
                 n = count_steps(z, self.delta_z)
                 if plen is not None and n > plen:
                     raise IndexError(f"the pump time profile has {plen} entries, the loop "
