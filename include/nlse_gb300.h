@@ -69,8 +69,10 @@ typedef struct {
  *   none), 6 vscale (V' = vscale * V).
  * [14], [15]: cos and sin of (omega/2)*dz for the Rabi rotation.
  * [30]: dz of the DDGPE pump term.
+ * [32], [33]: imaginary part of dz of set 0 and set 1 (imaginary-time
+ * evolution with a complex delta_z, NLSE/nlse.py:505-508; else 0).
  */
-#define NLSE_PARAM_STRIDE 32
+#define NLSE_PARAM_STRIDE 40
 
 /* The operator of one split step. */
 typedef struct {

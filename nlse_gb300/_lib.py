@@ -15,7 +15,7 @@ from . import _build
 NLSE_C64 = 0
 NLSE_C128 = 1
 NLSE_RUN_GRAPH = 1
-NLSE_PARAM_STRIDE = 32
+NLSE_PARAM_STRIDE = 40
 PASS_FORWARD, PASS_LINEAR, PASS_INV_NL_FWD, PASS_INV_NL = 0, 1, 2, 3
 
 OK = 0

@@ -13,7 +13,7 @@ import numpy as np
 import torch
 from scipy.constants import c, epsilon_0
 
-from . import engine
+from . import _lib, engine
 from .nlse import NLSE, __BACKEND__, _host
 
 
@@ -87,7 +87,7 @@ class CNLSE(NLSE):
         """Per-field, per-component parameters of nl_prop_c (cnlse.py:288-423)."""
         nf = int(np.prod(lead)) if lead else 1
         na = len(self._last_axes)
-        P = np.zeros((nf, 32), dtype=np.float64)
+        P = np.zeros((nf, _lib.NLSE_PARAM_STRIDE), dtype=np.float64)
         pf = lambda x, name: engine.per_field(x, lead, na, name)  # noqa: E731
         k, k2 = self.k, self.k2
         g11 = pf(k / 2 * _host(self.n2) * c * epsilon_0, "n2")
@@ -102,10 +102,13 @@ class CNLSE(NLSE):
         for s, dzs in ((0, dz / 2 if precision == "double" else dz), (1, dz / 2)):
             o = s * 16
             P[:, o + 0:o + 7] = np.stack(
-                [np.full(nf, dzs), a1, g11, g12, is1, is2, np.full(nf, k / 2)], axis=1)
+                [np.full(nf, np.real(dzs)), a1, g11, g12, is1, is2, np.full(nf, k / 2)], axis=1)
             P[:, o + 7:o + 14] = np.stack(
-                [np.full(nf, dzs), a2, g22, g21, is2, is1, np.full(nf, k2 / 2)], axis=1)
+                [np.full(nf, np.real(dzs)), a2, g22, g21, is2, is1, np.full(nf, k2 / 2)], axis=1)
+            P[:, 32 + s] = np.imag(dzs)
         if self.omega is not None:
+            if np.iscomplexobj(dz):
+                raise NotImplementedError("Rabi coupling with a complex delta_z")
             w = pf(_host(self.omega) / 2, "omega")
             P[:, 14] = np.cos(w * dz)
             P[:, 15] = np.sin(w * dz)

@@ -105,7 +105,8 @@ __global__ void k_nl_point(const StepArgs a) {
     const int64_t i0 = (f * NC) * a.pix + px;
     const cpx<T> x0 = A[i0];
     T a0 = (a.flags & F_ASQ_EXT) ? asq[i0] : abs2<T>(x0);
-    const NLP<T> p0 = load_nlp<T>(P);
+    NLP<T> p0 = load_nlp<T>(P);
+    p0.dzi = P[32];
     const int64_t vi = f * a.v_fstride + px;
     const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
     if constexpr (NC == 1) {
@@ -114,7 +115,8 @@ __global__ void k_nl_point(const StepArgs a) {
       const int64_t i1 = i0 + a.pix;
       const cpx<T> x1 = A[i1];
       const T a1 = (a.flags & F_ASQ_EXT) ? asq[i1] : abs2<T>(x1);
-      const NLP<T> p1 = load_nlp<T>(P + 7);
+      NLP<T> p1 = load_nlp<T>(P + 7);
+      p1.dzi = P[32];
       const cpx<T> v1 = has_v ? load_vp<T>(a.V, a.flags, vi, p1.vs) : mk<T>(T(0), T(0));
       cpx<T> y0 = nl_point<T>(x0, a0, a1, p0, has_v, v0);
       cpx<T> y1 = nl_point<T>(x1, a1, a0, p1, has_v, v1);
@@ -197,14 +199,16 @@ __global__ void k_nl_point_pad(const StepArgs a, const cpx<T>* __restrict__ X, i
     const cpx<T> c = X[(f * py + y) * px + x];
     const T* P = param_block<T>(a) + f * kParamStride + set * 16;
     const int64_t i0 = (f * NC) * a.pix + pxl;
-    const NLP<T> p0 = load_nlp<T>(P);
+    NLP<T> p0 = load_nlp<T>(P);
+    p0.dzi = param_block<T>(a)[f * kParamStride + 32 + set];
     const int64_t vi = f * a.v_fstride + pxl;
     const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
     if constexpr (NC == 1) {
       A[i0] = nl_point<T, false>(A[i0], c.x, T(0), p0, has_v, v0);
     } else {
       const int64_t i1 = i0 + a.pix;
-      const NLP<T> p1 = load_nlp<T>(P + 7);
+      NLP<T> p1 = load_nlp<T>(P + 7);
+      p1.dzi = p0.dzi;
       const cpx<T> v1 = has_v ? load_vp<T>(a.V, a.flags, vi, p1.vs) : mk<T>(T(0), T(0));
       cpx<T> y0 = nl_point<T>(A[i0], c.x, c.y, p0, has_v, v0);
       cpx<T> y1 = nl_point<T>(A[i1], c.y, c.x, p1, has_v, v1);

@@ -27,7 +27,7 @@ namespace nlse {
 //                            g_cross, isat_self, isat_cross, vscale
 //   [14], [15]              Rabi cos(omega*dz), sin(omega*dz)
 //   [30]                    dz used by the pump term
-constexpr int kParamStride = 32;
+constexpr int kParamStride = 40;
 
 enum : uint32_t {
   F_HAS_V = 1u << 0,      // potential present
@@ -102,6 +102,7 @@ struct ColArgs {
 template <typename T> struct NLP {
   T dz, alpha, gs, gc, is, ic, vs;
   T ris, ric;  // 1/is, 1/ic (per-thread reciprocals of the per-field constants)
+  T dzi;       // imaginary part of dz (imaginary-time evolution), else 0
 };
 
 // Parameters in the kernel's precision: complex64 kernels read the FP32
@@ -122,6 +123,7 @@ __device__ __forceinline__ NLP<T> load_nlp(const T* __restrict__ p) {
   r.vs = __ldg(p + 6);
   r.ris = T(1) / r.is;
   r.ric = T(1) / r.ic;
+  r.dzi = T(0);
   return r;
 }
 
@@ -226,8 +228,10 @@ __device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>&
     re = re - vp.y;
     im = im + vp.x;
   }
-  re = mul_rn(re, p.dz);
-  im = mul_rn(im, p.dz);
+  // (re + i im) * (dz + i dzi); with dzi = 0 exactly the rounded real products
+  const T re0 = re, im0 = im;
+  re = fma(-im0, p.dzi, mul_rn(re0, p.dz));
+  im = fma(re0, p.dzi, mul_rn(im0, p.dz));
   T cr, ci;
   cis_exp<T>(re, im, &cr, &ci);
   return cmul<T>(A, mk<T>(cr, ci));
@@ -308,11 +312,15 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
                                         int64_t f, int comp, int64_t pix0, int set, bool post,
                                         const VPre<E>* vpre = nullptr) {
   const T* P = param_block<T>(a) + f * kParamStride + set * 16;
-  const NLP<T> ps = load_nlp<T>(P + comp * 7);
+  NLP<T> ps = load_nlp<T>(P + comp * 7);
+  ps.dzi = __ldg(param_block<T>(a) + f * kParamStride + 32 + set);
   constexpr bool two = NC == 2;
   const bool rabi = two && post && (a.flags & F_RABI);
   NLP<T> po;
-  if (rabi) po = load_nlp<T>(P + (1 - comp) * 7);
+  if (rabi) {
+    po = load_nlp<T>(P + (1 - comp) * 7);
+    po.dzi = ps.dzi;
+  }
   const bool has_v = a.flags & F_HAS_V;
   const int64_t vb = f * a.v_fstride + pix0;
   const T* asq = reinterpret_cast<const T*>(a.asq);

@@ -14,7 +14,7 @@ from typing import Union
 import numpy as np
 import torch
 
-from . import engine
+from . import _lib, engine
 from .cnlse import CNLSE
 from .nlse import __BACKEND__, _host
 
@@ -119,8 +119,10 @@ class DDGPE(CNLSE):
         nf = int(np.prod(lead)) if lead else 1
         na = len(self._last_axes)
         pf = lambda x, name: engine.per_field(_host(x), lead, na, name)  # noqa: E731
-        P = np.zeros((nf, 32), dtype=np.float64)
+        P = np.zeros((nf, _lib.NLSE_PARAM_STRIDE), dtype=np.float64)
         dz = self.delta_z
+        if np.iscomplexobj(dz):
+            raise NotImplementedError("DDGPE with a complex delta_z")
         g, g2, g12 = pf(self.g, "g"), pf(self.g2, "g2"), pf(self.g12, "g12")
         is1, is2 = pf(self.I_sat, "Isat"), pf(self.I_sat2, "Isat2")
         ga1, ga2 = pf(_host(self.gamma) / 2, "gamma"), pf(_host(self.gamma2) / 2, "gamma2")

@@ -17,7 +17,7 @@ import torch
 from scipy import special
 from scipy.constants import c, epsilon_0
 
-from . import autotune, callbacks, engine
+from . import _lib, autotune, callbacks, engine
 from .engine import OperatorData, Plan
 
 __BACKEND__ = "GPU"
@@ -250,7 +250,7 @@ class NLSE:
         """
         nf = int(np.prod(lead)) if lead else 1
         na = len(self._last_axes)
-        P = np.zeros((nf, 32), dtype=np.float64)
+        P = np.zeros((nf, _lib.NLSE_PARAM_STRIDE), dtype=np.float64)
         dz = self.delta_z
         g = engine.per_field(self.k / 2 * _host(self.n2) * c * epsilon_0, lead, na, "n2")
         alpha = engine.per_field(_host(self.alpha) / 2, lead, na, "alpha")
@@ -258,7 +258,8 @@ class NLSE:
         vs = self.k / 2
         for s, dzs in ((0, dz / 2 if precision == "double" else dz), (1, dz / 2)):
             o = s * 16
-            P[:, o + 0] = dzs
+            P[:, o + 0] = np.real(dzs)
+            P[:, 32 + s] = np.imag(dzs)
             P[:, o + 1] = alpha
             P[:, o + 2] = g
             P[:, o + 3] = 0.0
@@ -278,8 +279,6 @@ class NLSE:
         dev = A.device
         lead = self._lead_shape(tuple(A.shape))
         na = len(self._last_axes)
-        if isinstance(self.delta_z, complex):
-            raise NotImplementedError("imaginary-time evolution (complex delta_z)")
         prop = engine.to_device(propagator, dev)
         if prop.dtype not in (torch.complex64, torch.complex128):
             prop = prop.to(torch.complex128 if A.dtype == torch.complex128 else torch.complex64)

@@ -3,6 +3,8 @@
 import numpy as np
 import pytest
 
+from nlse_gb300 import _lib
+
 from tests import golden_cases as gc
 from tests.cases import rel_l2
 
@@ -46,7 +48,7 @@ def test_elementwise_kernels_match_reference(tag):
     prop = torch.ones(1, dtype=torch.complex64, device=dev)
 
     def params(rows):
-        P = np.zeros((A.shape[0], 32))
+        P = np.zeros((A.shape[0], _lib.NLSE_PARAM_STRIDE))
         for k, row in rows.items():
             P[:, k:k + len(row)] = row
         return torch.from_numpy(P).to(dev)

@@ -133,7 +133,7 @@ def test_nlse_parameter_block_formulas():
     s = ng.NLSE(20, 1.05, 8.92e-3, -1.6e-9, None, 1e-2, NX=16, NY=16, Isat=1e5)
     s.delta_z = 5e-5
     P = s._nl_block((), "single", True)
-    assert P.shape == (1, 32)
+    assert P.shape == (1, _lib.NLSE_PARAM_STRIDE)
     assert P[0, 0] == 5e-5 and P[0, 1] == 10.0
     assert P[0, 2] == s.k / 2 * s.n2 * c * epsilon_0
     assert P[0, 4] == 2 * s.I_sat / (epsilon_0 * c) and np.isinf(P[0, 5])
