@@ -257,6 +257,15 @@ int nlse_power_noalloc(const void* A, int32_t dtype, int64_t nseg, int64_t seg_l
 int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64_t seg_len,
                    const double* sums, const double* target, double coef, void* stream);
 
+/* Complex Gaussian noise for the two components of DDGPE fields
+ * [nfields][2][pix] (replaces DDGPE.add_noise's random draws,
+ * NLSE/ddgpe.py:96-125): A[f][k][p] += sigma_k * (x + i y), x, y standard
+ * normals from a counter-based generator (Philox4x32-10 keyed by `seed`,
+ * counter (p, step)), the same for every field of the batch as the
+ * reference's (NY, NX) draw.  Reproducible for a given (seed, step). */
+int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double sigma0,
+                   double sigma1, uint64_t seed, int64_t step, void* stream);
+
 /* |A|^2 into a real array of the field precision (kernels_gpu.square_mod,
  * NLSE/kernels_gpu.py:179-190). */
 int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* stream);

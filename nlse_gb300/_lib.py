@@ -111,6 +111,12 @@ SIGNATURES = [
          ct.c_double, ct.c_void_p],
     ),
     ("nlse_square_mod", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_void_p]),
+    (
+        "nlse_add_noise",
+        ct.c_int,
+        [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_double, ct.c_double, ct.c_uint64,
+         ct.c_int64, ct.c_void_p],
+    ),
 ] + [
     # surrogate kernels (nlse_fno.h): p = pointer (device pointer or stream), l = int64,
     # i = int32, f = float

@@ -73,45 +73,51 @@ def adapt_delta_z(simu, A, z: float, i: int, update_every: int, delta_z: list) -
 # device copy into a preallocated slot).  Results reach the caller's arrays
 # once, after the loop.  No per-step host synchronisation.
 
-_DEVICE_KINDS = {}
-
-
-def device_plan(callback, callback_args):
-    """[(kind, save_every, destination)] if every callback can run as graph
-    nodes, else None (NLSE_DEVICE_CALLBACKS=0 turns this off)."""
+def device_plan(simu, callback, callback_args):
+    """[(kind, every, payload)] if every callback can run as graph nodes, else
+    None (NLSE_DEVICE_CALLBACKS=0 turns this off).  Kinds: "norm" and
+    "sample" (payload: the destination array) and, for DDGPE, "noise"
+    (payload: a function (A, step) adding that step's noise)."""
     import os
 
     if os.environ.get("NLSE_DEVICE_CALLBACKS", "") == "0":
         return None
-    if not _DEVICE_KINDS:
-        _DEVICE_KINDS.update({norm: "norm", sample: "sample"})
     if callable(callback):
         pairs = [(callback, callback_args)]
     elif isinstance(callback, list) and callback and all(callable(cb) for cb in callback):
         pairs = list(zip(callback, callback_args))
     else:
         return None
+    noise_fn = getattr(type(simu), "add_noise", None)
     out = []
     for cb, args in pairs:
-        kind = _DEVICE_KINDS.get(cb)
-        if kind is None or len(args) != 2 or int(args[0]) <= 0:
+        fn = getattr(cb, "__func__", cb)
+        if fn is norm or fn is sample:
+            if len(args) != 2 or int(args[0]) <= 0:
+                return None
+            out.append(("norm" if fn is norm else "sample", int(args[0]), args[1]))
+        elif noise_fn is not None and fn is noise_fn and hasattr(simu, "_add_noise"):
+            amp = float(args[0]) if len(args) else 0.0
+            simu._noise_sigmas(amp)  # raises here, not inside a capture, if unsupported
+            out.append(("noise", 1, lambda A, step, amp=amp: simu._add_noise(A, step, amp)))
+        else:
             return None
-        out.append((kind, int(args[0]), args[1]))
     return out
 
 
 def run_in_graph(plan, A: torch.Tensor, op, n: int, recs) -> bool:
-    """Advance A by n steps with the recordings of recs as graph nodes; False
+    """Advance A by n steps with the callbacks of recs as graph nodes; False
     (nothing done) if the recording buffers would not fit comfortably."""
-    counts = [len(range(0, n, s)) for _, s, _ in recs]
+    store = [(k, s, d) for k, s, d in recs if k != "noise"]
+    counts = [len(range(0, n, s)) for _, s, _ in store]
     need = sum(c * (A.numel() * A.element_size() if k == "sample" else 8)
-               for (k, _, _), c in zip(recs, counts))
+               for (k, _, _), c in zip(store, counts))
     free, _ = torch.cuda.mem_get_info(A.device)
     if need > free // 4:
         return False
     bufs = [torch.empty((c,) + (tuple(A.shape) if k == "sample" else ()),
                         dtype=A.dtype if k == "sample" else torch.float64, device=A.device)
-            for (k, _, _), c in zip(recs, counts)]
+            for (k, _, _), c in zip(store, counts)]
     points = sorted({i for _, s, _ in recs for i in range(0, n, s)})
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
@@ -119,7 +125,13 @@ def run_in_graph(plan, A: torch.Tensor, op, n: int, recs) -> bool:
         for p in points:
             engine.propagate(plan, A, op, p + 1 - i0, i0, graph=False)
             i0 = p + 1
-            for (kind, s, _), buf in zip(recs, bufs):
+            j = 0
+            for kind, s, payload in recs:  # in the callbacks' order
+                if kind == "noise":
+                    payload(A, p)
+                    continue
+                buf = bufs[j]
+                j += 1
                 if p % s == 0:
                     if kind == "norm":
                         buf[p // s].copy_(engine.power(A, 1)[0])
@@ -128,7 +140,7 @@ def run_in_graph(plan, A: torch.Tensor, op, n: int, recs) -> bool:
         if i0 < n:
             engine.propagate(plan, A, op, n - i0, i0, graph=False)
     g.replay()
-    for (kind, _, dst), buf in zip(recs, bufs):
+    for (kind, _, dst), buf in zip(store, bufs):
         for j in range(buf.shape[0]):
-            _store(dst, j, buf[j] if kind == "sample" else buf[j])
+            _store(dst, j, buf[j])
     return True

@@ -1047,6 +1047,18 @@ int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* st
   return NLSE_OK;
 }
 
+int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double sigma0,
+                   double sigma1, uint64_t seed, int64_t step, void* stream) {
+  g_err.clear();
+  if (!A || nfields <= 0 || pix <= 0 || step < 0 || step > 0xFFFFFFFFll ||
+      (dtype != NLSE_C64 && dtype != NLSE_C128))
+    return fail(NLSE_ERR_ARG, "nlse_add_noise: bad argument");
+  cudaError_t e = launch_add_noise(dtype, A, nfields, pix, sigma0, sigma1, seed, (uint32_t)step,
+                                   reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "add_noise");
+  return NLSE_OK;
+}
+
 }  // extern "C"
 
 namespace {

@@ -34,6 +34,8 @@ cudaError_t launch_scale(int dtype, const void* in, void* out, int64_t nseg, int
                          const double* sums, const double* target, double coef, cudaStream_t s);
 cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStream_t s);
+cudaError_t launch_add_noise(int dtype, void* A, int64_t nfields, int64_t pix, double s0, double s1,
+                             uint64_t seed, uint32_t step, cudaStream_t s);
 cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t s);
 // Nonlocal response: pack |A|^2 into the padded scratch, multiply by the
 // kernel spectrum, nonlinear step reading the convolved intensities.

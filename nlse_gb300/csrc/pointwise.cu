@@ -407,4 +407,71 @@ cudaError_t launch_nl_pointwise(int dtype, const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---- counter-based Gaussian noise (DDGPE.add_noise) --------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC 2011): a keyed bijection of a 128-bit counter, ten rounds of
+// two 32 x 32 -> 64-bit multiplies and a Weyl key schedule.  Key = the 64-bit
+// seed; counter = (pixel, step, 0, 0).  The four outputs become four standard
+// normals by two Box-Muller transforms: (re, im) of component 0 and of
+// component 1 at that pixel and step.
+struct Philox4 {
+  uint32_t v[4];
+};
+
+__host__ __device__ inline Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                 uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)M0 * c0, p1 = (uint64_t)M1 * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += W0;
+    k1 += W1;
+  }
+  return Philox4{{c0, c1, c2, c3}};
+}
+
+// uniform in (0, 1) from 32 random bits
+__device__ __forceinline__ float u01(uint32_t x) { return ((float)x + 0.5f) * 2.3283064365386963e-10f; }
+
+template <typename T>
+__global__ void k_add_noise(cpx<T>* __restrict__ A, int64_t nfields, int64_t pix, T s0, T s1,
+                            uint32_t k0, uint32_t k1, uint32_t step) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pix;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const Philox4 r = philox4x32_10((uint32_t)p, step, (uint32_t)(p >> 32), 0u, k0, k1);
+    float sn, cs;
+    const float ra = sqrtf(-2.f * logf(u01(r.v[0])));
+    sincospif(2.f * u01(r.v[1]), &sn, &cs);
+    const T n0r = T(ra * cs), n0i = T(ra * sn);
+    const float rb = sqrtf(-2.f * logf(u01(r.v[2])));
+    sincospif(2.f * u01(r.v[3]), &sn, &cs);
+    const T n1r = T(rb * cs), n1i = T(rb * sn);
+    for (int64_t f = 0; f < nfields; ++f) {
+      cpx<T>* a0 = A + (f * 2) * pix + p;
+      cpx<T>* a1 = a0 + pix;
+      *a0 = mk<T>(a0->x + s0 * n0r, a0->y + s0 * n0i);
+      *a1 = mk<T>(a1->x + s1 * n1r, a1->y + s1 * n1i);
+    }
+  }
+}
+
+cudaError_t launch_add_noise(int dtype, void* A, int64_t nfields, int64_t pix, double s0, double s1,
+                             uint64_t seed, uint32_t step, cudaStream_t s) {
+  const int64_t blocks = (pix + 255) / 256 < 4096 ? (pix + 255) / 256 : 4096;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  if (dtype == 0)  // complex64
+    k_add_noise<float><<<(unsigned)blocks, 256, 0, s>>>(reinterpret_cast<float2*>(A), nfields, pix,
+                                                        (float)s0, (float)s1, k0, k1, step);
+  else
+    k_add_noise<double><<<(unsigned)blocks, 256, 0, s>>>(reinterpret_cast<double2*>(A), nfields,
+                                                         pix, s0, s1, k0, k1, step);
+  return cudaGetLastError();
+}
+
 }  // namespace nlse

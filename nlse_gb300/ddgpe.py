@@ -59,6 +59,9 @@ class DDGPE(CNLSE):
             (omega_exc - omega_cav) ** 2 + (omega) ** 2)
         self.omega_pump = omega_lp + detuning
         self._random = self._device_normal
+        # add_noise draws from the library's counter-based generator keyed by
+        # this seed and the step index: the same seed gives the same noise
+        self.noise_seed = 0
 
     _DEVICE_ATTRS = ("power", "n2", "alpha", "I_sat", "n22", "n12", "gamma", "g", "omega",
                      "k_z", "omega_exc", "omega_cav", "detuning", "omega_pump")
@@ -70,16 +73,39 @@ class DDGPE(CNLSE):
 
     @staticmethod
     def add_noise(simu, A, t, i, noise: float = 0) -> None:
-        """Noise callback (ddgpe.py:96-125), on the device field."""
-        shape = (simu.NY, simu.NX)
-        rand1 = simu._random(loc=0, scale=simu.delta_z, size=shape) + 1j * simu._random(
-            loc=0, scale=simu.delta_z, size=shape)
-        rand2 = simu._random(loc=0, scale=simu.delta_z, size=shape) + 1j * simu._random(
-            loc=0, scale=simu.delta_z, size=shape)
-        A[..., 0, :, :] += (noise * np.sqrt(simu.gamma / (4 * (simu.delta_X * simu.delta_Y)))
-                            * rand1).to(A.dtype)
-        A[..., 1, :, :] += (noise * np.sqrt(simu.gamma2 / (4 * (simu.delta_X * simu.delta_Y)))
-                            * rand2).to(A.dtype)
+        """Noise callback (ddgpe.py:96-125) on the device field.
+
+        Adds complex Gaussian noise of standard deviation delta_z per
+        quadrature, scaled by noise * sqrt(gamma_k / (4 dX dY)) on component k,
+        as the reference; the draws come from nlse_add_noise (Philox4x32-10
+        keyed by simu.noise_seed, counter = pixel and step i), so they are
+        reproducible and the same for every field of a batch, like the
+        reference's (NY, NX) draw broadcast over the batch.
+        """
+        simu._add_noise(A, i, noise)
+
+    def _noise_sigmas(self, noise: float) -> tuple:
+        out = []
+        for gam in (self.gamma, self.gamma2):
+            g = np.asarray(_host(gam), dtype=np.float64).reshape(-1)
+            if g.size != 1:
+                raise NotImplementedError("add_noise with per-field gamma")
+            if np.iscomplexobj(self.delta_z):
+                raise NotImplementedError("add_noise with a complex delta_z")
+            out.append(float(noise * np.sqrt(g[0] / (4 * (self.delta_X * self.delta_Y)))
+                             * self.delta_z))
+        return tuple(out)
+
+    def _add_noise(self, A, i: int, noise: float) -> None:
+        engine.require_cuda(A)
+        s0, s1 = self._noise_sigmas(noise)
+        lead = self._lead_shape(tuple(A.shape))
+        nf = int(np.prod(lead)) if lead else 1
+        lib = _lib.load()
+        with torch.cuda.device(A.device):
+            _lib.check(lib.nlse_add_noise(A.data_ptr(), engine.dtype_code(A), nf,
+                                          self.NY * self.NX, s0, s1, int(self.noise_seed) & (2**64 - 1),
+                                          int(i), engine.stream_handle(A.device)), "add_noise")
 
     @staticmethod
     def laser_excitation(simu, A, t, i, F_pump_r, F_pump_t, F_probe_r, F_probe_t) -> None:

@@ -385,14 +385,17 @@ class NLSE:
             if z > self.L:
                 self.n2 = 0
             plen = None if pump is None else min(pump[1].numel(), pump[3].numel())
-            recs = None if callback is None or pump is not None else callbacks.device_plan(
-                callback, callback_args)
+            recs = None if callback is None else callbacks.device_plan(
+                self, callback, callback_args)
             if recs is not None:
-                # norm / sample callbacks as nodes of one graph over the whole loop
+                # device callbacks as nodes of one graph over the whole loop
                 n = count_steps(z, self.delta_z)
+                if plen is not None and n > plen:
+                    raise IndexError(f"the pump time profile has {plen} entries, the loop "
+                                     f"runs {n} steps")
                 done = n == 0
                 if n > 0:
-                    op = self._operator(A, V, self.propagator, precision, None, self.plans[0])
+                    op = self._operator(A, V, self.propagator, precision, pump, self.plans[0])
                     autotune.maybe_tune(self.plans[0], A, op)
                     done = callbacks.run_in_graph(self.plans[0], A, op, n, recs)
                 if done:

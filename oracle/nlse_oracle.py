@@ -506,3 +506,32 @@ class OracleDDGPE(OracleCNLSE):
                         else self.laser_excitation)
         return super().out_field(E_in, t, precision=precision, normalize=False,
                                  callback=callback, callback_args=callback_args)
+
+
+# ---- counter-based noise (test oracle of nlse_add_noise) ----------------------
+def philox4x32_10(c, k0, k1):
+    """Philox4x32-10 (Salmon et al., SC 2011) on arrays of 4 uint32 counters
+    c = (c0, c1, c2, c3) with key (k0, k1); returns the four output words."""
+    M0, M1, W0, W1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57), 0x9E3779B9, 0xBB67AE85
+    c0, c1, c2, c3 = (np.asarray(x, np.uint64) for x in c)
+    k0, k1 = int(k0), int(k1)
+    mask = np.uint64(0xFFFFFFFF)
+    for _ in range(10):
+        p0, p1 = M0 * c0, M1 * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
+        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
+        c0, c1, c2, c3 = (hi1 ^ c1 ^ np.uint64(k0)), lo1, (hi0 ^ c3 ^ np.uint64(k1)), lo0
+        k0, k1 = (k0 + W0) & 0xFFFFFFFF, (k1 + W1) & 0xFFFFFFFF
+    return c0, c1, c2, c3
+
+
+def ddgpe_noise(pix: int, seed: int, step: int):
+    """Standard complex normals (component 0, component 1) per pixel for one step."""
+    p = np.arange(pix, dtype=np.uint64)
+    r = philox4x32_10((p & np.uint64(0xFFFFFFFF), np.full(pix, step, np.uint64),
+                       p >> np.uint64(32), np.zeros(pix, np.uint64)),
+                      seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
+    u = [(x.astype(np.float64) + 0.5) * 2.0**-32 for x in r]
+    ra, rb = np.sqrt(-2 * np.log(u[0])), np.sqrt(-2 * np.log(u[2]))
+    return (ra * np.cos(2 * np.pi * u[1]) + 1j * ra * np.sin(2 * np.pi * u[1]),
+            rb * np.cos(2 * np.pi * u[3]) + 1j * rb * np.sin(2 * np.pi * u[3]))
