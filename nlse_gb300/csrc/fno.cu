@@ -8,7 +8,7 @@
 //   s_l     = (1/N^2) Re( sum_{k in R} S_l(k) exp(+2 pi i k.x / N) )
 //   S_l(k)  = bf16(H_l(k)) . bf16(W_l(k))        per-mode 32 x 32 complex mixing
 //   H_l(k)  = sum_x h_l(x) exp(-2 pi i k.x / N)  truncated transform
-//   h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)
+//   h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)   GELU in its tanh form
 //   out     = h_4 . Wp + bp                      two channels: Re, Im of E(L)
 // The truncated transforms run on the project's Stockham FFT (fft_core.cuh):
 // 256-point row transforms of channel pairs packed as one complex line, and
@@ -50,12 +50,22 @@ constexpr size_t kPairBuf =
     (16 * SL > N * PS ? 16 * SL : N * PS) * sizeof(float2);  // shared by xl and the pairs
 
 __device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+// GELU in its tanh form, 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3),
+// with the hardware tanh (relative error ~2^-11, below the BF16 rounding of
+// the stored activations)
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluA = 0.7978845608028654f, kGeluB = 0.044715f;
 __device__ __forceinline__ float gelu(float z) {
-  return 0.5f * z * (1.f + erff(z * 0.70710678118654752f));
+  const float t = tanh_hw(kGeluA * fmaf(kGeluB * z, z * z, z));
+  return 0.5f * z * (1.f + t);
 }
 __device__ __forceinline__ float gelu_grad(float z) {
-  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) +
-         z * 0.39894228040143268f * expf(-0.5f * z * z);
+  const float t = tanh_hw(kGeluA * fmaf(kGeluB * z, z * z, z));
+  return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluA * fmaf(3.f * kGeluB, z * z, 1.f);
 }
 // kept row iy (0..63) of ky
 __device__ __forceinline__ int iy_of(int ky) { return ky < KY / 2 ? ky : ky - (N - KY); }
@@ -363,7 +373,7 @@ __device__ __forceinline__ void issue_row_conv(uint32_t tbase, const __nv_bfloat
   umma_commit(&st->bar);
 }
 
-__global__ void __launch_bounds__(256) k_layer_rows(const LayerArgs a) {
+__global__ void __launch_bounds__(256, 4) k_layer_rows(const LayerArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   float2* xl = reinterpret_cast<float2*>(smraw);
   float2* ss = xl;

@@ -12,7 +12,7 @@ modes kx in [0, 32), ky in [0, 32) u [224, 256) (mode index iy*32 + kx).
     S_l     = bf16(H_l) . bf16(W_l)         per mode, complex 32 x 32
     s_l     = Re(ifft2(zero-filled S_l))    ((1/N^2) Re sum_k S(k) e^{+ik.x})
     z_l     = h_l . bf16(Wc_l) + s_l + b_l
-    h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)
+    h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)   (tanh-form GELU)
     out     = h_4 . Wp + bp                 (Re, Im)
 
 Gradients pass through the bf16() roundings unchanged.  With exact=True no
@@ -22,7 +22,6 @@ rounding is applied (for finite-difference checks of the gradients).
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 N, C, KX, KY, NL = 256, 32, 32, 64, 4
 NM = KX * KY
@@ -41,12 +40,17 @@ def bf16c(z: np.ndarray) -> np.ndarray:
     return bf16(z.real) + 1j * bf16(z.imag)
 
 
+GA, GB = np.sqrt(2.0 / np.pi), 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU in its tanh form (the kernels' activation)."""
+    return 0.5 * z * (1.0 + np.tanh(GA * (z + GB * z**3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    t = np.tanh(GA * (z + GB * z**3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GA * (1.0 + 3.0 * GB * z * z)
 
 
 def analysis(h: np.ndarray) -> np.ndarray:
