@@ -180,7 +180,40 @@ template <int N, int EREQ = 16> struct Shape {
 // (b / NS) * NS * R + (b % NS) + r * NS.
 constexpr int TWG = 4;  // twiddles loaded per group
 
-template <typename T, int N, int E, int R, int NS, bool INV>
+// Compact twiddle table of one N-point transform (E points per thread): the
+// tables of its twiddled passes (NS > 1) back to back, [r-1][k] each.
+__host__ __device__ constexpr int tw_compact_offset(int n, int e, int upto_ns) {
+  int off = 0;
+  for (int ns = 1; ns < upto_ns && ns < n;) {
+    const int rmax = e < 16 ? e : 16;
+    const int r = (n / ns) >= rmax ? rmax : n / ns;
+    if (r < 2) break;
+    if (ns > 1) off += (r - 1) * ns;
+    ns *= r;
+  }
+  return off;
+}
+__host__ __device__ constexpr int tw_compact_len(int n, int e) { return tw_compact_offset(n, e, n); }
+
+// Copy the compact table of an N-point transform from the full table (all threads).
+template <typename T, int N, int E>
+__device__ __forceinline__ void load_tw_compact(cpx<T>* dst, const cpx<T>* __restrict__ tw) {
+  int ns = 1;
+#pragma unroll 1
+  while (ns < N) {
+    const int rmax = E < 16 ? E : 16;
+    const int r = (N / ns) >= rmax ? rmax : N / ns;
+    if (ns > 1) {
+      const int off = tw_compact_offset(N, E, ns), len = (r - 1) * ns;
+      for (int i = threadIdx.x; i < len; i += blockDim.x) dst[off + i] = tw[tw_offset(r, ns) + i];
+    }
+    ns *= r;
+  }
+}
+
+// TWS: tw is a compact table in shared memory (load_tw_compact) instead of
+// the full table in global memory.
+template <typename T, int N, int E, int R, int NS, bool INV, bool TWS = false>
 __device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T>* __restrict__ tw) {
   constexpr int TPL = N / E, BPT = E / R;
   static_assert(NS * R <= kTwMaxLen, "twiddle tables cover sub-transforms up to kTwMaxLen");
@@ -195,13 +228,15 @@ __device__ __forceinline__ void stockham_pass(cpx<T> (&x)[E], int t, const cpx<T
       // loads are merged with the forward ones and ~30 values stay live in
       // registers across both transforms (register spills).
       asm volatile("" : "+r"(k)::"memory");
-      const cpx<T>* twp = tw + tw_offset(R, NS) + k;
+      const cpx<T>* twp = tw + (TWS ? tw_compact_offset(N, E, NS) : tw_offset(R, NS)) + k;
 #pragma unroll
       for (int r = 1; r < R; ++r) {
         // load and apply the twiddles in groups of TWG so that at most TWG
         // of them are live at once (bounds register pressure)
         if (r > 1 && (r - 1) % TWG == 0) asm volatile("" ::: "memory");
-        cpx<T> w = __ldg(twp + (r - 1) * NS);
+        cpx<T> w;
+        if constexpr (TWS) w = twp[(r - 1) * NS];
+        else w = __ldg(twp + (r - 1) * NS);
         if (INV) w.y = -w.y;
         y[r] = cmul<T>(y[r], w);
       }
@@ -288,7 +323,7 @@ __device__ __forceinline__ void fence_async_after_stores() {
 
 // FENCE: the exchange buffer is also a bulk-copy staging buffer that is
 // refilled later, so the exchange stores are fenced against that copy.
-template <typename T, int N, int E, int NS, bool INV, bool FENCE = false>
+template <typename T, int N, int E, int NS, bool INV, bool FENCE = false, bool TWS = false>
 __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int stride,
                                          const cpx<T>* __restrict__ tw) {
   constexpr int R = PassRadix<N, E, NS>::R;
@@ -298,14 +333,14 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
     // keeping those of an earlier transform in this kernel live in registers.
     asm volatile("" : "+r"(t)::"memory");
   }
-  stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
+  stockham_pass<T, N, E, R, NS, INV, TWS>(x, t, tw);
   if constexpr (NS * R < N) {
     __syncthreads();
     exchange_store<T, N, E, NS>(x, t, sm, stride);
     if constexpr (FENCE) fence_async_after_stores();
     __syncthreads();
     exchange_load<T, N, E>(x, t, sm, stride);
-    fft_line<T, N, E, NS * R, INV, FENCE>(x, t, sm, stride, tw);
+    fft_line<T, N, E, NS * R, INV, FENCE, TWS>(x, t, sm, stride, tw);
   }
 }
 
@@ -316,20 +351,20 @@ __device__ __forceinline__ void fft_line(cpx<T> (&x)[E], int t, cpx<T>* sm, int 
 // of exchanges the last one uses B, so A is free once the transform returns.
 // FM: bit 0 / bit 1 fence the stores into A / B (buffers that later receive
 // bulk copies).
-template <typename T, int N, int E, int NS, bool INV, int P, int FM>
+template <typename T, int N, int E, int NS, bool INV, int P, int FM, bool TWS = false>
 __device__ __forceinline__ void fft_line_db(cpx<T> (&x)[E], int t, cpx<T>* smA, cpx<T>* smB,
                                             int stride, const cpx<T>* __restrict__ tw) {
   constexpr int R = PassRadix<N, E, NS>::R;
   static_assert((E / R) * R == E, "radix must divide the elements per thread");
   if constexpr (NS == 1) asm volatile("" : "+r"(t)::"memory");
-  stockham_pass<T, N, E, R, NS, INV>(x, t, tw);
+  stockham_pass<T, N, E, R, NS, INV, TWS>(x, t, tw);
   if constexpr (NS * R < N) {
     cpx<T>* sm = P ? smB : smA;
     exchange_store<T, N, E, NS>(x, t, sm, stride);
     if constexpr ((FM >> P) & 1) fence_async_after_stores();
     __syncthreads();
     exchange_load<T, N, E>(x, t, sm, stride);
-    fft_line_db<T, N, E, NS * R, INV, P ^ 1, FM>(x, t, smA, smB, stride, tw);
+    fft_line_db<T, N, E, NS * R, INV, P ^ 1, FM, TWS>(x, t, smA, smB, stride, tw);
   }
 }
 

@@ -746,12 +746,24 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E)) k_cols_blk(const ColArgs
 // engine brings tile i + gridDim.x into the other stage.  Results go straight
 // back to global memory (coalesced stores).  Same arithmetic as k_cols_blk.
 constexpr int kColStages = 2;
+constexpr size_t kMaxSmemBytes = 227 * 1024;  // dynamic shared memory a CTA may opt into
 
 template <typename T, int N>
-__host__ __device__ constexpr size_t cols_tma_smem() {
+__host__ __device__ constexpr size_t cols_tma_base_smem() {
   // kColStages staging tiles and one exchange tile, each padded
   return (size_t)(kColStages + 1) * stage_len<T>(padded_len(N) * BlkW<T>::W) * sizeof(cpx<T>) +
          kColStages * sizeof(uint64_t);
+}
+// The column pass keeps its transform's twiddles in shared memory when they fit.
+template <typename T, int N>
+__host__ __device__ constexpr bool cols_tma_tws() {
+  return cols_tma_base_smem<T, N>() + (size_t)tw_compact_len(N, Shape<N>::E) * sizeof(cpx<T>) + 16 <=
+         kMaxSmemBytes;
+}
+template <typename T, int N>
+__host__ __device__ constexpr size_t cols_tma_smem() {
+  return cols_tma_base_smem<T, N>() +
+         (cols_tma_tws<T, N>() ? (size_t)tw_compact_len(N, Shape<N>::E) * sizeof(cpx<T>) + 16 : 0);
 }
 
 template <typename T, int N, int E, bool PC128>
@@ -770,7 +782,11 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
   C* stage = reinterpret_cast<C*>(smraw);
   C* xch = stage + kColStages * SLW;
   uint64_t* bar = reinterpret_cast<uint64_t*>(xch + SLW);
-  const C* tw = reinterpret_cast<const C*>(a.tw);
+  // the transform's twiddles, copied once per CTA into shared memory when they fit
+  constexpr bool TWS = cols_tma_tws<T, N>();
+  C* twc = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(bar) + 16);
+  if constexpr (TWS) load_tw_compact<T, N, E>(twc, reinterpret_cast<const C*>(a.tw));
+  const C* tw = TWS ? twc : reinterpret_cast<const C*>(a.tw);
   C* S = reinterpret_cast<C*>(a.A);
   const int c = threadIdx.x % W, t = threadIdx.x / W;
   const int64_t ntiles = a.nblocks;
@@ -835,10 +851,10 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
     __syncthreads();  // every thread has read stage st
     C* sA = stage + st * SLW + c;
     if constexpr (DB) {
-      fft_line_db<T, N, E, 1, false, 0, 1>(x, t, sA, xch + c, W, tw);
+      fft_line_db<T, N, E, 1, false, 0, 1, TWS>(x, t, sA, xch + c, W, tw);
     } else {
       if (threadIdx.x == 0) refill(st, i);
-      fft_line<T, N, E, 1, false>(x, t, xch + c, W, tw);
+      fft_line<T, N, E, 1, false, false, TWS>(x, t, xch + c, W, tw);
     }
     if constexpr (PC128) {
 #pragma unroll
@@ -848,11 +864,11 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
       for (int j = 0; j < E; ++j) x[j] = cmul<T>(x[j], mk<T>(T(pre[j].x), T(pre[j].y)));
     }
     if constexpr (DB) {
-      fft_line_db<T, N, E, 1, true, 0, 1>(x, t, sA, xch + c, W, tw);
+      fft_line_db<T, N, E, 1, true, 0, 1, TWS>(x, t, sA, xch + c, W, tw);
       // the last exchange used xch, so every read of stage st is behind a barrier
       if (threadIdx.x == 0) refill(st, i);
     } else {
-      fft_line<T, N, E, 1, true>(x, t, xch + c, W, tw);
+      fft_line<T, N, E, 1, true, false, TWS>(x, t, xch + c, W, tw);
     }
     C* g = S + o * a.outer_stride + toff;
 #pragma unroll
