@@ -266,6 +266,35 @@ int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64
 int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double sigma0,
                    double sigma1, uint64_t seed, int64_t step, void* stream);
 
+/* Nonlinear refractive-index change of the callbacks (NLSE/callbacks.py).
+ * The field is nseg segments of pix points; coef, n2abs and isat are device
+ * arrays of nseg doubles (one value per segment: per field and component).
+ * Evaluated as NumPy evaluates the callbacks' expressions, operation by
+ * operation without contraction:
+ *   q  = re*re + im*im                          (nlse_delta_n)
+ *   q  = re*re + ((im*im*c)*eps0)/2             (nlse_delta_n_max, the
+ *        precedence of adapt_delta_z, callbacks.py:109)
+ *   dn = (coef * q) / (1 + q / isat)
+ * in the field precision, except that flag NLSE_DN_COEF_F64 evaluates
+ * coef * q and NLSE_DN_ISAT_F64 evaluates 1 + q / isat in FP64 (parameters
+ * NumPy treats as float64 rather than as weak scalars); the quotient is FP64
+ * if either is.  c and eps0 are rounded to the field precision. */
+#define NLSE_DN_COEF_F64 1
+#define NLSE_DN_ISAT_F64 2
+
+/* evaluate_delta_n (NLSE/callbacks.py:57-82): out[s][p] = dn with
+ * coef_s = c*eps0/2*n2 (computed by the caller); out is float32 for a
+ * complex64 field without flags, float64 otherwise. */
+int nlse_delta_n(const void* A, int32_t dtype, int64_t nseg, int64_t pix, const double* coef,
+                 const double* isat, int32_t flags, void* out, void* stream);
+
+/* adapt_delta_z's peak (NLSE/callbacks.py:85-112): *out (device double) =
+ * max over all points of dn with coef_s = |n2_s|; a NaN anywhere gives NaN,
+ * as NumPy's max.  Stream-ordered; the caller reads *out when it needs it. */
+int nlse_delta_n_max(const void* A, int32_t dtype, int64_t nseg, int64_t pix, const double* n2abs,
+                     const double* isat, double c, double eps0, int32_t flags, double* out,
+                     void* stream);
+
 /* |A|^2 into a real array of the field precision (kernels_gpu.square_mod,
  * NLSE/kernels_gpu.py:179-190). */
 int nlse_square_mod(const void* A, void* out, int32_t dtype, int64_t n, void* stream);

@@ -17,6 +17,7 @@ NLSE_C128 = 1
 NLSE_RUN_GRAPH = 1
 NLSE_PARAM_STRIDE = 40
 PASS_FORWARD, PASS_LINEAR, PASS_INV_NL_FWD, PASS_INV_NL = 0, 1, 2, 3
+DN_COEF_F64, DN_ISAT_F64 = 1, 2
 
 OK = 0
 ERR_ARG = -1
@@ -116,6 +117,18 @@ SIGNATURES = [
         ct.c_int,
         [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_double, ct.c_double, ct.c_uint64,
          ct.c_int64, ct.c_void_p],
+    ),
+    (
+        "nlse_delta_n",
+        ct.c_int,
+        [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_int32,
+         ct.c_void_p, ct.c_void_p],
+    ),
+    (
+        "nlse_delta_n_max",
+        ct.c_int,
+        [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_double,
+         ct.c_double, ct.c_int32, ct.c_void_p, ct.c_void_p],
     ),
 ] + [
     # surrogate kernels (nlse_fno.h): p = pointer (device pointer or stream), l = int64,

@@ -1059,6 +1059,31 @@ int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double 
   return NLSE_OK;
 }
 
+int nlse_delta_n(const void* A, int32_t dtype, int64_t nseg, int64_t pix, const double* coef,
+                 const double* isat, int32_t flags, void* out, void* stream) {
+  g_err.clear();
+  if (!A || !coef || !isat || !out || nseg <= 0 || pix <= 0 || (flags & ~3) ||
+      (dtype != NLSE_C64 && dtype != NLSE_C128))
+    return fail(NLSE_ERR_ARG, "nlse_delta_n: bad argument");
+  cudaError_t e = launch_delta_n(dtype, A, nseg, pix, coef, isat, flags, out,
+                                 reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "delta_n");
+  return NLSE_OK;
+}
+
+int nlse_delta_n_max(const void* A, int32_t dtype, int64_t nseg, int64_t pix, const double* n2abs,
+                     const double* isat, double c, double eps0, int32_t flags, double* out,
+                     void* stream) {
+  g_err.clear();
+  if (!A || !n2abs || !isat || !out || nseg <= 0 || pix <= 0 || (flags & ~3) ||
+      (dtype != NLSE_C64 && dtype != NLSE_C128))
+    return fail(NLSE_ERR_ARG, "nlse_delta_n_max: bad argument");
+  cudaError_t e = launch_delta_n_max(dtype, A, nseg, pix, n2abs, isat, c, eps0, flags, out,
+                                     reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "delta_n_max");
+  return NLSE_OK;
+}
+
 }  // extern "C"
 
 namespace {

@@ -37,6 +37,14 @@ cudaError_t launch_abs2(int dtype, const void* A, void* out, int64_t n, cudaStre
 cudaError_t launch_add_noise(int dtype, void* A, int64_t nfields, int64_t pix, double s0, double s1,
                              uint64_t seed, uint32_t step, cudaStream_t s);
 cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t s);
+// Nonlinear index change of the callbacks (flags: 1 = coef * |A|^2 in FP64,
+// 2 = 1 + |A|^2 / isat in FP64); out is float unless a flag is set or the
+// field is complex128.  The max variant writes one double to out.
+cudaError_t launch_delta_n(int dtype, const void* A, int64_t nseg, int64_t pix, const double* coef,
+                           const double* isat, int flags, void* out, cudaStream_t s);
+cudaError_t launch_delta_n_max(int dtype, const void* A, int64_t nseg, int64_t pix,
+                               const double* n2abs, const double* isat, double c, double eps0,
+                               int flags, double* out, cudaStream_t s);
 // Nonlocal response: pack |A|^2 into the padded scratch, multiply by the
 // kernel spectrum, nonlinear step reading the convolved intensities.
 cudaError_t launch_pack_asq(int dtype, int nc, const void* A, void* X, int64_t nfields, int64_t ny,

@@ -1,6 +1,8 @@
 // Pointwise and reduction kernels: FP64 power sums, power normalisation,
-// the standalone nonlinear operator and |A|^2.
+// the standalone nonlinear operator, |A|^2, the DDGPE noise and the
+// callbacks' nonlinear index change.
 #include <mutex>
+#include <type_traits>
 
 #include "launch.h"
 
@@ -471,6 +473,152 @@ cudaError_t launch_add_noise(int dtype, void* A, int64_t nfields, int64_t pix, d
   else
     k_add_noise<double><<<(unsigned)blocks, 256, 0, s>>>(reinterpret_cast<double2*>(A), nfields,
                                                          pix, s0, s1, k0, k1, step);
+  return cudaGetLastError();
+}
+
+// ---- nonlinear index change (callbacks evaluate_delta_n / adapt_delta_z) ----
+// NumPy's evaluation of the callbacks' expressions, operation by operation:
+// every product, sum and quotient rounded on its own (no contraction), a
+// parameter NumPy treats as a weak scalar rounded once to the field
+// precision, a float64 parameter (array or NumPy scalar) widening the
+// operations it enters.  TC: precision of coef * |A|^2; TD: of 1 + |A|^2/isat.
+__device__ __forceinline__ float dn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double dn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float dn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double dn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float dn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double dn_div(double a, double b) { return __ddiv_rn(a, b); }
+
+// |A|^2 as the callback writes it: evaluate_delta_n (callbacks.py:80)
+// re*re + im*im; adapt_delta_z (callbacks.py:109) re*re + ((im*im*c)*eps0)/2,
+// where by operator precedence c*eps0/2 scales only the imaginary square.
+template <typename T, bool ADAPT>
+__device__ __forceinline__ T dn_asq(cpx<T> a, T c, T eps0) {
+  const T r2 = dn_mul(a.x, a.x);
+  T i2 = dn_mul(a.y, a.y);
+  if (ADAPT) i2 = dn_div(dn_mul(dn_mul(i2, c), eps0), T(2));
+  return dn_add(r2, i2);
+}
+
+template <typename T, typename TC, typename TD, bool ADAPT>
+__device__ __forceinline__ typename std::conditional<(sizeof(TC) > sizeof(TD)), TC, TD>::type
+dn_value(cpx<T> a, double coef, double isat, T c, T eps0) {
+  using TO = typename std::conditional<(sizeof(TC) > sizeof(TD)), TC, TD>::type;
+  const T q = dn_asq<T, ADAPT>(a, c, eps0);
+  const TC num = dn_mul(TC(coef), TC(q));
+  const TD den = dn_add(TD(1), dn_div(TD(q), TD(isat)));
+  return dn_div(TO(num), TO(den));
+}
+
+template <typename T, typename TC, typename TD>
+__global__ void k_delta_n(const cpx<T>* __restrict__ A, int64_t nseg, int64_t pix,
+                          const double* __restrict__ coef, const double* __restrict__ isat,
+                          typename std::conditional<(sizeof(TC) > sizeof(TD)), TC, TD>::type* out) {
+  for (int64_t sg = blockIdx.y; sg < nseg; sg += gridDim.y) {
+    const double cf = coef[sg], is = isat[sg];
+    const int64_t b = sg * pix;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pix;
+         p += (int64_t)gridDim.x * blockDim.x)
+      out[b + p] = dn_value<T, TC, TD, false>(A[b + p], cf, is, T(0), T(0));
+  }
+}
+
+// Order-preserving map of a double onto uint64, every NaN mapped above +inf
+// (to all ones, which maps back to a NaN).  The maximum is taken on these
+// keys with integer compares only, so no floating-point compare can drop a
+// NaN.
+__device__ __forceinline__ unsigned long long dn_key(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return ~0ull;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+template <typename T, typename TC, typename TD>
+__global__ void k_delta_n_max(const cpx<T>* __restrict__ A, int64_t nseg, int64_t pix,
+                              const double* __restrict__ n2abs, const double* __restrict__ isat,
+                              T c, T eps0, unsigned long long* key) {
+  unsigned long long k = 0ull;  // below every key
+  for (int64_t sg = blockIdx.y; sg < nseg; sg += gridDim.y) {
+    const double cf = n2abs[sg], is = isat[sg];
+    const int64_t b = sg * pix;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pix;
+         p += (int64_t)gridDim.x * blockDim.x) {
+      const unsigned long long q = dn_key(double(dn_value<T, TC, TD, true>(A[b + p], cf, is, c, eps0)));
+      k = q > k ? q : k;  // a NaN wins, as in NumPy's max
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long q = __shfl_xor_sync(0xffffffffu, k, o);
+    k = q > k ? q : k;
+  }
+  __shared__ unsigned long long wk[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wk[warp] = k;
+  __syncthreads();
+  if (warp == 0) {
+    k = lane < (int)(blockDim.x >> 5) ? wk[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long q = __shfl_xor_sync(0xffffffffu, k, o);
+      k = q > k ? q : k;
+    }
+    if (lane == 0) atomicMax(key, k);
+  }
+}
+
+__global__ void k_key_to_double(unsigned long long* key) {
+  const unsigned long long k = *key;
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  *reinterpret_cast<double*>(key) = __longlong_as_double((long long)b);
+}
+
+static dim3 dn_grid(int64_t nseg, int64_t pix) {
+  const int64_t bx = (pix + 255) / 256;
+  const int64_t gx = bx < 1216 ? bx : 1216;  // 8 blocks of 256 per SM on 152 SMs
+  const int64_t gy = nseg < 65535 ? nseg : 65535;
+  return dim3((unsigned)gx, (unsigned)gy);
+}
+
+cudaError_t launch_delta_n(int dtype, const void* A, int64_t nseg, int64_t pix, const double* coef,
+                           const double* isat, int flags, void* out, cudaStream_t s) {
+  const dim3 g = dn_grid(nseg, pix);
+  const bool c64 = flags & 1, d64 = flags & 2;
+  if (dtype == 1) {
+    k_delta_n<double, double, double><<<g, 256, 0, s>>>(reinterpret_cast<const double2*>(A), nseg,
+                                                        pix, coef, isat, (double*)out);
+  } else {
+    const float2* a = reinterpret_cast<const float2*>(A);
+    if (c64 && d64) k_delta_n<float, double, double><<<g, 256, 0, s>>>(a, nseg, pix, coef, isat, (double*)out);
+    else if (c64) k_delta_n<float, double, float><<<g, 256, 0, s>>>(a, nseg, pix, coef, isat, (double*)out);
+    else if (d64) k_delta_n<float, float, double><<<g, 256, 0, s>>>(a, nseg, pix, coef, isat, (double*)out);
+    else k_delta_n<float, float, float><<<g, 256, 0, s>>>(a, nseg, pix, coef, isat, (float*)out);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_delta_n_max(int dtype, const void* A, int64_t nseg, int64_t pix,
+                               const double* n2abs, const double* isat, double c, double eps0,
+                               int flags, double* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const dim3 g = dn_grid(nseg, pix);
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(out);
+  const bool c64 = flags & 1, d64 = flags & 2;
+  if (dtype == 1) {
+    k_delta_n_max<double, double, double><<<g, 256, 0, s>>>(reinterpret_cast<const double2*>(A),
+                                                            nseg, pix, n2abs, isat, c, eps0, key);
+  } else {
+    const float2* a = reinterpret_cast<const float2*>(A);
+    const float cf = (float)c, ef = (float)eps0;
+    if (c64 && d64) k_delta_n_max<float, double, double><<<g, 256, 0, s>>>(a, nseg, pix, n2abs, isat, cf, ef, key);
+    else if (c64) k_delta_n_max<float, double, float><<<g, 256, 0, s>>>(a, nseg, pix, n2abs, isat, cf, ef, key);
+    else if (d64) k_delta_n_max<float, float, double><<<g, 256, 0, s>>>(a, nseg, pix, n2abs, isat, cf, ef, key);
+    else k_delta_n_max<float, float, float><<<g, 256, 0, s>>>(a, nseg, pix, n2abs, isat, cf, ef, key);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_key_to_double<<<1, 1, 0, s>>>(key);
   return cudaGetLastError();
 }
 

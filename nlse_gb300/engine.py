@@ -219,6 +219,36 @@ def power(A: torch.Tensor, nseg: int) -> torch.Tensor:
     return out
 
 
+def delta_n(A: torch.Tensor, pix: int, coef: torch.Tensor, isat: torch.Tensor, flags: int,
+            out: torch.Tensor) -> None:
+    """evaluate_delta_n's index change of A into out (nlse_delta_n); coef and
+    isat: FP64 device values per segment of pix points."""
+    require_cuda(A)
+    nseg = A.numel() // pix
+    want = torch.float64 if (flags or A.dtype == torch.complex128) else torch.float32
+    if out.dtype != want or out.numel() != A.numel() or not out.is_contiguous():
+        raise ValueError(f"delta_n output must be a contiguous {want} array of the field's size")
+    with torch.cuda.device(A.device):
+        _lib.check(_lib.load().nlse_delta_n(A.data_ptr(), dtype_code(A), nseg, pix,
+                                            coef.data_ptr(), isat.data_ptr(), int(flags),
+                                            out.data_ptr(), stream_handle(A.device)), "delta_n")
+
+
+def delta_n_max(A: torch.Tensor, pix: int, n2abs: torch.Tensor, isat: torch.Tensor, c: float,
+                eps0: float, flags: int, out: torch.Tensor) -> None:
+    """adapt_delta_z's peak index change of A into the FP64 device scalar out
+    (nlse_delta_n_max); stream-ordered, nothing is read back here."""
+    require_cuda(A)
+    nseg = A.numel() // pix
+    if out.dtype != torch.float64 or out.numel() < 1:
+        raise ValueError("delta_n_max writes one float64 value")
+    with torch.cuda.device(A.device):
+        _lib.check(_lib.load().nlse_delta_n_max(A.data_ptr(), dtype_code(A), nseg, pix,
+                                                n2abs.data_ptr(), isat.data_ptr(), float(c),
+                                                float(eps0), int(flags), out.data_ptr(),
+                                                stream_handle(A.device)), "delta_n_max")
+
+
 def normalize(src: torch.Tensor, dst: torch.Tensor, nseg: int, sums: torch.Tensor,
               target: torch.Tensor, coef: float) -> None:
     """dst = src * sqrt(target / (sums * coef)) per segment (nlse_normalize)."""

@@ -388,16 +388,30 @@ class NLSE:
             recs = None if callback is None else callbacks.device_plan(
                 self, callback, callback_args)
             if recs is not None:
-                # device callbacks as nodes of one graph over the whole loop
+                # device callbacks: nodes of one graph over the whole loop, or
+                # graph segments between the updates of an adaptive step
                 n = count_steps(z, self.delta_z)
-                if plen is not None and n > plen:
+                adaptive = any(k == "adapt" for k, _, _ in recs)
+                if plen is not None and n > plen and not adaptive:
                     raise IndexError(f"the pump time profile has {plen} entries, the loop "
                                      f"runs {n} steps")
                 done = n == 0
-                if n > 0:
+                if adaptive:
+                    # the step count follows the adapted step: segments between updates
                     op = self._operator(A, V, self.propagator, precision, pump, self.plans[0])
                     autotune.maybe_tune(self.plans[0], A, op)
-                    done = callbacks.run_in_graph(self.plans[0], A, op, n, recs)
+                    lead = self._lead_shape(tuple(A.shape))
+                    has_v = V is not None
+
+                    def refresh(op=op, lead=lead, has_v=has_v):
+                        op.params.copy_(torch.from_numpy(self._nl_block(lead, precision, has_v)))
+
+                    done = callbacks.run_adaptive(self, self.plans[0], A, op, z, recs, refresh,
+                                                  plen)
+                elif n > 0:
+                    op = self._operator(A, V, self.propagator, precision, pump, self.plans[0])
+                    autotune.maybe_tune(self.plans[0], A, op)
+                    done = callbacks.run_in_graph(self, self.plans[0], A, op, n, recs)
                 if done:
                     callback = None
             if callback is None and recs is not None:

@@ -535,3 +535,30 @@ def ddgpe_noise(pix: int, seed: int, step: int):
     ra, rb = np.sqrt(-2 * np.log(u[0])), np.sqrt(-2 * np.log(u[2]))
     return (ra * np.cos(2 * np.pi * u[1]) + 1j * ra * np.sin(2 * np.pi * u[1]),
             rb * np.cos(2 * np.pi * u[3]) + 1j * rb * np.sin(2 * np.pi * u[3]))
+
+
+# ---------------------------------------------------------------------------
+# callbacks' nonlinear index change (NLSE/callbacks.py:57-112)
+# ---------------------------------------------------------------------------
+def delta_n(A, n2, I_sat):
+    """evaluate_delta_n's record (NLSE/callbacks.py:79-82): NumPy evaluation of
+    c*eps0/2*n2*|A|^2 / (1 + |A|^2/I_sat) with |A|^2 = re*re + im*im, every
+    operation rounded on its own, Python-float parameters weak (field
+    precision), float64 arrays and NumPy scalars strong."""
+    a_sq = A.real * A.real + A.imag * A.imag
+    return c * epsilon_0 / 2 * n2 * a_sq / (1 + a_sq / I_sat)
+
+
+def adapt_peak(A, n2, I_sat):
+    """Peak of adapt_delta_z's index change (NLSE/callbacks.py:108-110); the
+    factor c*eps0/2 multiplies only the imaginary square there (operator
+    precedence), and np.abs of a Python float is a float64 NumPy scalar."""
+    a_sq = A.real * A.real + A.imag * A.imag * c * epsilon_0 / 2
+    return (np.abs(n2) * a_sq / (1 + a_sq / I_sat)).max()
+
+
+def adapt_delta_z(A, n2, I_sat, k):
+    """The step adapt_delta_z sets (NLSE/callbacks.py:110-112)."""
+    with np.errstate(divide="ignore"):
+        z_nl = float(1 / (k * adapt_peak(A, n2, I_sat)))
+    return np.abs(z_nl) / 12

@@ -220,6 +220,51 @@ def run_nlse2d(R, name, N, dtype, precision, noise=0.0, with_v=True, dz=5e-5, NY
          power=np.asarray(power), precision=np.array(precision))
 
 
+def run_callbacks(R, name, N, dtype, precision, batch=None, adapt_every=0, every=4, z=2e-3,
+                  dz=5e-5):
+    """out_field with the reference's own callbacks: sample + evaluate_delta_n +
+    norm every `every` steps, or sample + adapt_delta_z every `adapt_every`
+    steps (sample first, so the samples hold the field each update saw)."""
+    from NLSE import callbacks as rcb
+
+    n2, power = N2, POWER
+    if batch:
+        n2 = np.linspace(-1.6e-9, -4e-10, batch).reshape(batch, 1, 1)
+        power = np.linspace(0.5, 2.0, batch)
+    sim = R.NLSE(ALPHA, power, WINDOW, n2, None, L, NX=N, NY=N, Isat=ISAT, backend="GPU")
+    sim.delta_z = dz
+    E = gauss(sim.XX, sim.YY).astype(np.complex128)
+    if batch:
+        E = np.broadcast_to(E, (batch, N, N)).copy()
+    E = E.astype(dtype)
+    sim.V = well(sim.XX, sim.YY).astype(np.complex64)
+    cnt = Counter()
+    if adapt_every:
+        nrec = 64
+        samples = np.zeros((nrec,) + E.shape, dtype=dtype)
+        dzs = []
+        out = sim.out_field(E, z, precision=precision, verbose=False,
+                            callback=[rcb.sample, rcb.adapt_delta_z, cnt],
+                            callback_args=[(adapt_every, samples), (adapt_every, dzs), ()])
+        nrec = (cnt.n - 1) // adapt_every + 1
+        save(name, E_in=E, V=sim.V, out=out, samples=samples[:nrec], dzs=np.array(dzs),
+             meta=np.array([N, dz, z, cnt.n, adapt_every, sim.k]), n2=np.asarray(n2),
+             power=np.asarray(power), precision=np.array(precision))
+        return
+    nrec = (int(round(z / dz)) + every) // every + 1
+    samples = np.zeros((nrec,) + E.shape, dtype=dtype)
+    rdt = np.float64 if (batch or dtype == np.complex128) else np.float32
+    dn = np.zeros((nrec,) + E.shape, dtype=rdt)
+    norms = np.zeros(nrec)
+    out = sim.out_field(E, z, precision=precision, verbose=False,
+                        callback=[rcb.sample, rcb.evaluate_delta_n, rcb.norm, cnt],
+                        callback_args=[(every, samples), (every, dn), (every, norms), ()])
+    nrec = (cnt.n - 1) // every + 1
+    save(name, E_in=E, V=sim.V, out=out, samples=samples[:nrec], delta_n=dn[:nrec],
+         norms=norms[:nrec], meta=np.array([N, dz, z, cnt.n, every, sim.k]), n2=np.asarray(n2),
+         power=np.asarray(power), precision=np.array(precision))
+
+
 def main() -> None:
     import os
     import tempfile
@@ -244,6 +289,13 @@ def main() -> None:
                dz=1e-4)
     run_nlse2d(R, "nlse2d_c128_nonlocal_double", 64, np.complex128, "double", nl_length=300e-6,
                dz=1e-4)
+    # the reference's callbacks (NLSE/callbacks.py) inside out_field
+    run_callbacks(R, "callbacks_c64_delta_n", 32, np.complex64, "single")
+    run_callbacks(R, "callbacks_c64_batch_delta_n", 32, np.complex64, "single", batch=3)
+    run_callbacks(R, "callbacks_c128_delta_n", 32, np.complex128, "double")
+    run_callbacks(R, "callbacks_c64_adapt", 32, np.complex64, "single", adapt_every=4)
+    run_callbacks(R, "callbacks_c128_adapt", 32, np.complex128, "single", adapt_every=3)
+
     # the reference's CPU path (numba kernels run as Python loops: tiny case)
     run_nlse2d(R, "nlse2d_cpu_c128_single", 16, np.complex128, "single", backend="CPU", dz=1e-3)
 

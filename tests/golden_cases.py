@@ -16,7 +16,7 @@ WAIST, WAIST2, POWER, N2, ISAT, ALPHA, L = 2.23e-3, 70e-6, 1.05, -1.6e-9, 1e5, 2
 WINDOW = 4 * WAIST
 
 FIXTURES = sorted(p.stem for p in GOLDEN.glob("*.npz")
-                  if not p.stem.startswith(("kernels_", "step_counts")))
+                  if not p.stem.startswith(("kernels_", "step_counts", "callbacks_")))
 
 
 def load(name: str) -> dict:
