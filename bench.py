@@ -316,21 +316,31 @@ def run_gb300(args):
     value = world * B * args.steps / t
     launches = 1 + 2 * args.steps
 
-    # per-kernel durations on the launching stream (torch's current stream)
-    def time_pass(which, reps=20):
+    # per-kernel durations on the launching stream (torch's current stream),
+    # inside the same (column pass, row pass) sequence the loop runs: an event
+    # after every launch.  (A pass repeated on its own runs at other speeds:
+    # the row pass 230-275 us instead of ~214 us, as its L2 contents differ.)
+    def time_passes(reps=20):
+        engine.run_pass(plan, A, op, _lib.PASS_FORWARD)
         for _ in range(3):
-            engine.run_pass(plan, A, op, which)
+            engine.run_pass(plan, A, op, _lib.PASS_LINEAR)
+            engine.run_pass(plan, A, op, _lib.PASS_INV_NL_FWD)
         torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(reps):
-            engine.run_pass(plan, A, op, which)
-        b.record()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps + 1)]
+        evs[0].record()
+        for i in range(reps):
+            engine.run_pass(plan, A, op, _lib.PASS_LINEAR)
+            evs[2 * i + 1].record()
+            engine.run_pass(plan, A, op, _lib.PASS_INV_NL_FWD)
+            evs[2 * i + 2].record()
+        engine.run_pass(plan, A, op, _lib.PASS_LINEAR)
+        engine.run_pass(plan, A, op, _lib.PASS_INV_NL)
         torch.cuda.synchronize()
-        return a.elapsed_time(b) / reps / 1e3
+        col = sum(evs[2 * i].elapsed_time(evs[2 * i + 1]) for i in range(reps)) / reps
+        row = sum(evs[2 * i + 1].elapsed_time(evs[2 * i + 2]) for i in range(reps)) / reps
+        return col / 1e3, row / 1e3
 
-    t_col = time_pass(_lib.PASS_LINEAR)
-    t_row = time_pass(_lib.PASS_INV_NL_FWD)
+    t_col, t_row = time_passes()
     npix = N * N * B
     peak, peak_kind = peaks()
     kern = {
