@@ -407,6 +407,48 @@ def run_gb300(args):
         single = {"steps": ng.count_steps(L, DZ), "steps_per_s": ng.count_steps(L, DZ) / min(ts),
                   "note": "one 2048^2 field, 501-step out_field loop from device memory, "
                           "L2 flushed between loops (the field itself fits in L2)"}
+
+        def loop_time(sim, E, z, reps=3):
+            sim.out_field(E, z, verbose=False)
+            torch.cuda.synchronize()
+            best = None
+            for _ in range(reps):
+                flush.fill_(1)
+                a.record()
+                sim.out_field(E, z, verbose=False)
+                b.record()
+                torch.cuda.synchronize()
+                t_ = a.elapsed_time(b) / 1e3
+                best = t_ if best is None else min(best, t_)
+            return best
+
+        # the same loop in complex128 (the configuration's FP64 run); real FP32 potential:
+        # 3 sweeps x 2 x 16 B + 4 B per point and step
+        E1d = torch.from_numpy(E_host[0].astype(np.complex128)).to(dev)
+        td = loop_time(s1, E1d, L)
+        nst1 = ng.count_steps(L, DZ)
+        single_c128 = {"steps": nst1, "steps_per_s": nst1 / td,
+                       "gbs_100B_per_pt": round(100 * N * N * nst1 / td / 1e9, 1),
+                       "note": "one 2048^2 complex128 field, 501-step out_field loop from "
+                               "device memory, L2 flushed between loops"}
+        # the coupled 1024^2 configuration: CNLSE, both components, Gaussian nonlocal
+        # kernel (sigma 100 um on a 67^2 support), L = 20 mm at dz = 5e-5 (400 steps)
+        NC, LC = 1024, 20e-3
+        s3 = ng.CNLSE(ALPHA, 0.5, 4 * WAIST, N2, -0.8e-9, None, LC, NX=NC, NY=NC, Isat=ISAT,
+                      nl_length=100e-6)
+        s3.delta_z, s3.power2, s3.n22 = 5e-5, 0.05, N2
+        dxc = 4 * WAIST / NC
+        rr = np.arange(-33, 34) * dxc
+        kern = np.exp(-(rr[:, None] ** 2 + rr[None, :] ** 2) / (2 * (100e-6) ** 2))
+        s3.nl_profile = kern / kern.sum()
+        E3 = np.array([np.exp(-(s3.XX**2 + s3.YY**2) / w**2) for w in (1.5e-3, 0.5e-3)])
+        E3 = torch.from_numpy(E3.astype(np.complex64)).to(dev)
+        tc = loop_time(s3, E3, LC)
+        nst3 = ng.count_steps(LC, 5e-5)
+        cnlse = {"steps": nst3, "steps_per_s": nst3 / tc,
+                 "note": "CNLSE 1024^2 complex64, two components, Gaussian nonlocal kernel "
+                         "(linear convolution on a zero-padded 2048^2 grid every step), "
+                         "400-step out_field loop from device memory, L2 flushed between loops"}
     # the 164-field mixed batch (96 @ 256^2, 48 @ 512^2, 16 @ 1024^2, 4 @ 2048^2), one
     # grouped graph launch for the whole loop; inputs resident on the device
     from tests import cases
@@ -450,7 +492,8 @@ def run_gb300(args):
                            "l2": "inputs larger than L2 (256 MiB per GPU)",
                            "step_model_gbs_52B_per_pt": round(step_model_gbs, 1),
                            "kernel_variant": tuned,
-                           "single_field_loop": single, "mixed_batch_164": mixed,
+                           "single_field_loop": single, "single_field_loop_c128": single_c128,
+                           "cnlse_1024_nonlocal": cnlse, "mixed_batch_164": mixed,
                            "surrogate_256": sur},
                 "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks}
