@@ -96,9 +96,9 @@ def out_fields(jobs, z: float, precision: str = "single", normalize: bool = True
     for simu, E_in, A, *_ in prepared:
         simu._retrieve_arrays_from_gpu()
         if isinstance(E_in, np.ndarray):
-            out.append(A.cpu().numpy())
+            out.append(engine.to_host(A).numpy())
         elif isinstance(E_in, torch.Tensor) and not E_in.is_cuda:
-            out.append(A.cpu())
+            out.append(engine.to_host(A))
         else:
             out.append(A)
     return out

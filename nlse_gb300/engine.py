@@ -10,6 +10,7 @@ from __future__ import annotations
 import ctypes as ct
 import itertools
 import math
+import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -333,6 +334,41 @@ def nonlocal_spectrum(profile, grid: tuple, dtype: torch.dtype, device) -> tuple
     plan = Plan.get(len(pads), pads, 1, 1, dtype_code(khat), device)
     plan.fft(khat)
     return pads, khat.contiguous()
+
+
+_STAGE: dict = {}
+_STAGE_LOCK = threading.Lock()
+STAGE_MIN_BYTES = 8 << 20
+
+
+def to_host(t: torch.Tensor) -> torch.Tensor:
+    """A new host tensor with the values of t.  Large device tensors go
+    through a pinned staging buffer kept per device (the device copy at the
+    pinned rate, then torch's multi-threaded host copy): a direct copy into
+    new pageable memory runs at about a tenth of that.  release_staging()
+    returns the buffers."""
+    if not t.is_cuda or t.numel() * t.element_size() < STAGE_MIN_BYTES:
+        return t.cpu()
+    t = t.contiguous()
+    nbytes = t.numel() * t.element_size()
+    with _STAGE_LOCK:
+        key = t.device.index
+        buf = _STAGE.get(key)
+        if buf is None or buf.numel() < nbytes:
+            _STAGE.pop(key, None)
+            buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+            _STAGE[key] = buf
+        view = buf[:nbytes].view(t.dtype).view(t.shape)
+        view.copy_(t)  # waits for the producing stream
+        out = torch.empty(t.shape, dtype=t.dtype)
+        out.copy_(view)
+    return out
+
+
+def release_staging() -> None:
+    """Free the pinned staging buffers of to_host."""
+    with _STAGE_LOCK:
+        _STAGE.clear()
 
 
 def to_device(x, device, dtype=None) -> torch.Tensor:

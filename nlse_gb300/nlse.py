@@ -220,27 +220,35 @@ class NLSE:
         Records which of them were host arrays: only those go back to the host
         afterwards (device tensors a caller supplied stay where they are)."""
         dev = self._device
-        host = set()
+        host = {}
         for name in ("V", "nl_profile", "propagator"):
             v = getattr(self, name, None)
             if v is not None:
+                t = engine.to_device(v, dev)
                 if not _is_device_array(v):
-                    host.add(name)
-                setattr(self, name, engine.to_device(v, dev))
+                    host[name] = (v, t, t._version)
+                setattr(self, name, t)
         for name in self._DEVICE_ATTRS:
             v = getattr(self, name, None)
             if isinstance(v, np.ndarray):
-                host.add(name)
-                setattr(self, name, engine.to_device(v, dev))
+                t = engine.to_device(v, dev)
+                host[name] = (v, t, t._version)
+                setattr(self, name, t)
         self._host_attrs = host
 
     def _retrieve_arrays_from_gpu(self) -> None:
-        """Bring the arrays that were host arrays back to NumPy (nlse.py:344-370)."""
-        for name in getattr(self, "_host_attrs", ()):
+        """Bring the arrays that were host arrays back to NumPy (nlse.py:344-370).
+
+        A device copy that nothing changed in place (its torch version counter
+        is the one it had when sent) gives back the caller's own host array,
+        which holds the same values, without a copy; a changed one is copied."""
+        for name, (orig, t, ver) in getattr(self, "_host_attrs", {}).items():
             v = getattr(self, name, None)
-            if _is_device_array(v):
-                setattr(self, name, v.cpu().numpy())
-        self._host_attrs = set()
+            if v is t and t._version == ver:
+                setattr(self, name, orig)
+            elif _is_device_array(v):
+                setattr(self, name, engine.to_host(v).numpy())
+        self._host_attrs = {}
 
     # -- the split-step operator --------------------------------------------
     def _nl_block(self, lead: tuple, precision: str, has_v: bool) -> np.ndarray:
@@ -459,9 +467,9 @@ class NLSE:
                   f" {time.perf_counter() - t0} s (CPU)\n")
         self._retrieve_arrays_from_gpu()
         if isinstance(E_in, np.ndarray):
-            return A.cpu().numpy()
+            return engine.to_host(A).numpy()
         if isinstance(E_in, torch.Tensor) and not E_in.is_cuda:
-            return A.cpu()
+            return engine.to_host(A)
         return A
 
     def _op_key(self):
