@@ -266,6 +266,14 @@ int nlse_normalize(const void* in, void* out, int32_t dtype, int64_t nseg, int64
 int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double sigma0,
                    double sigma1, uint64_t seed, int64_t step, void* stream);
 
+/* Self-test of the bounded waits (no reference counterpart): one CTA waits
+ * on an mbarrier that nothing completes, with the loop every wait of the
+ * passes uses, and gives up after limit_ns (at most 1 s, the passes' limit).
+ * On giving up it stores the device timeout code (1) into *status, as the
+ * passes store it into a plan's status word, and the wait's duration into
+ * *elapsed_ns (both device pointers).  The context stays usable. */
+int nlse_wait_selftest(int32_t* status, uint64_t* elapsed_ns, int64_t limit_ns, void* stream);
+
 /* Nonlinear refractive-index change of the callbacks (NLSE/callbacks.py).
  * The field is nseg segments of pix points; coef, n2abs and isat are device
  * arrays of nseg doubles (one value per segment: per field and component).

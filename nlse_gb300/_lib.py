@@ -118,6 +118,7 @@ SIGNATURES = [
         [ct.c_void_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.c_double, ct.c_double, ct.c_uint64,
          ct.c_int64, ct.c_void_p],
     ),
+    ("nlse_wait_selftest", ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_void_p]),
     (
         "nlse_delta_n",
         ct.c_int,

@@ -1059,6 +1059,18 @@ int nlse_add_noise(void* A, int32_t dtype, int64_t nfields, int64_t pix, double 
   return NLSE_OK;
 }
 
+int nlse_wait_selftest(int32_t* status, uint64_t* elapsed_ns, int64_t limit_ns, void* stream) {
+  g_err.clear();
+  if (!status || !elapsed_ns || limit_ns <= 0 || limit_ns > (int64_t)kWaitLimitNs)
+    return fail(NLSE_ERR_ARG, "nlse_wait_selftest: limit must be in (0, 1 s]");
+  cudaError_t e = launch_wait_selftest(reinterpret_cast<int*>(status),
+                                       reinterpret_cast<unsigned long long*>(elapsed_ns),
+                                       (unsigned long long)limit_ns,
+                                       reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "wait_selftest");
+  return NLSE_OK;
+}
+
 int nlse_delta_n(const void* A, int32_t dtype, int64_t nseg, int64_t pix, const double* coef,
                  const double* isat, int32_t flags, void* out, void* stream) {
   g_err.clear();

@@ -40,6 +40,9 @@ cudaError_t launch_params_f32(const double* p, float* q, int64_t n, cudaStream_t
 // Nonlinear index change of the callbacks (flags: 1 = coef * |A|^2 in FP64,
 // 2 = 1 + |A|^2 / isat in FP64); out is float unless a flag is set or the
 // field is complex128.  The max variant writes one double to out.
+// One CTA waits on an mbarrier nothing completes, giving up after limit_ns.
+cudaError_t launch_wait_selftest(int* status, unsigned long long* elapsed_ns,
+                                 unsigned long long limit_ns, cudaStream_t s);
 cudaError_t launch_delta_n(int dtype, const void* A, int64_t nseg, int64_t pix, const double* coef,
                            const double* isat, int flags, void* out, cudaStream_t s);
 cudaError_t launch_delta_n_max(int dtype, const void* A, int64_t nseg, int64_t pix,

@@ -476,6 +476,33 @@ cudaError_t launch_add_noise(int dtype, void* A, int64_t nfields, int64_t pix, d
   return cudaGetLastError();
 }
 
+// ---- bounded-wait self-test ---------------------------------------------------
+// A wait that nothing ends: an mbarrier expecting one arrival that never
+// comes, waited on with a limit of limit_ns (the same loop as every wait of
+// the passes); the outcome goes to status the way the passes report it, so
+// the host sees the timeout path work and the context stay usable.
+__global__ void k_wait_selftest(int* status, unsigned long long* elapsed_ns,
+                                unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned long long t0 = global_ns();
+    const bool ok = mbar_wait_limit(&bar, 0, limit_ns);
+    *elapsed_ns = global_ns() - t0;
+    if (!ok) atomicExch(status, DEV_WAIT_TIMEOUT);
+  }
+}
+
+cudaError_t launch_wait_selftest(int* status, unsigned long long* elapsed_ns,
+                                 unsigned long long limit_ns, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(status, elapsed_ns, limit_ns);
+  return cudaGetLastError();
+}
+
 // ---- nonlinear index change (callbacks evaluate_delta_n / adapt_delta_z) ----
 // NumPy's evaluation of the callbacks' expressions, operation by operation:
 // every product, sum and quotient rounded on its own (no contraction), a

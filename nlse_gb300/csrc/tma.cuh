@@ -57,14 +57,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return done != 0;
 }
 
-// Wait for phase `parity` of the barrier; false if the deadline passed first.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+// Polls after which a wait gives up even if the timer should not advance
+// (each poll is a try_wait, which may itself suspend for a while).
+constexpr unsigned kWaitMaxPolls = 1u << 26;
+
+// Wait for phase `parity` of the barrier; false if limit_ns passed first.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, unsigned parity,
+                                                unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > kWaitLimitNs) return false;
-  }
+  for (unsigned n = 0; !mbar_try_wait(bar, parity); ++n)
+    if (global_ns() - t0 > limit_ns || n > kWaitMaxPolls) return false;
   return true;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  return mbar_wait_limit(bar, parity, kWaitLimitNs);
 }
 
 // Contiguous global -> shared bulk copy completing on `bar` (sizes and both
