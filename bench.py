@@ -253,6 +253,74 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GB300 path
 # ---------------------------------------------------------------------------
+def gpu_stand_in(dev, E_host, V, sim, plan, op, steps=20, warmup=3):
+    """The reference's GPU-path step, measured as a stand-in for its VkFFT path.
+
+    The reference's GPU path needs cupy and pyvkfft, which are not installed,
+    so its arithmetic is restated here on torch.fft (cuFFT) and torch
+    elementwise operations, step by step as NLSE.split_step "single" runs it
+    (nlse.py:372-487): forward 2-D FFT, times the propagator, inverse FFT
+    (normalised), square_mod (kernels_gpu.py:179-190: |A|**2), nl_prop
+    (kernels_gpu.py:4-37).  Baseline only; the product never uses cuFFT.  The
+    elementwise part is unfused here (cupy fuses it into one kernel), so the
+    FFT + propagator part is also reported alone as a bound the reference
+    cannot beat.  A cross-check compares its field with the product's after
+    the same steps."""
+    import torch
+    from scipy.constants import c, epsilon_0
+
+    from nlse_gb300 import engine
+
+    A0 = torch.from_numpy(E_host).to(dev)
+    P = sim.propagator
+    P = (P if isinstance(P, torch.Tensor) else torch.from_numpy(np.asarray(P))).to(dev)
+    Vk = torch.from_numpy(np.asarray(sim.k / 2 * V)).to(dev)
+    g = sim.k / 2 * N2 * c * epsilon_0
+    isat = 2 * ISAT / (epsilon_0 * c)
+    a2 = ALPHA / 2
+
+    def step(A):
+        A = torch.fft.ifft2(torch.fft.fft2(A).mul_(P))
+        A_sq = torch.abs(A) ** 2
+        sat = 1 / (1 + A_sq / isat)
+        arg = 1j * g * A_sq * sat
+        arg = arg - a2 * sat
+        arg = arg + 1j * Vk
+        arg = arg * DZ
+        return A.mul_(torch.exp(arg))
+
+    def fft_part(A):
+        return torch.fft.ifft2(torch.fft.fft2(A).mul_(P))
+
+    def timed(f):
+        A = A0.clone()
+        for _ in range(warmup):
+            A = f(A)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(steps):
+            A = f(A)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / steps
+
+    t_step, t_fft = timed(step), timed(fft_part)
+    # the same steps on the product, from the same field
+    A = A0.clone()
+    for _ in range(steps):
+        A0 = step(A0)
+    engine.propagate(plan, A, op, steps, 0, graph=False)
+    torch.cuda.synchronize()
+    err = float(torch.linalg.vector_norm(A - A0) / torch.linalg.vector_norm(A0))
+    nf = E_host.shape[0]
+    return {"field_steps_per_s": nf / t_step, "fft_and_propagator_only_field_steps_per_s": nf / t_fft,
+            "rel_l2_vs_product_after_steps": err, "steps_compared": steps,
+            "note": "reference VkFFT GPU path unavailable (cupy and pyvkfft are not installed); "
+                    "stand-in: the reference's split_step arithmetic on torch.fft (cuFFT) and "
+                    "unfused torch elementwise ops, same 8-field 2048^2 workload, device-resident"}
+
+
 def run_gb300(args):
     import torch
 
@@ -478,6 +546,9 @@ def run_gb300(args):
     mixed = {"fields": 164, "steps": nb, "field_steps_per_s": world * 164 * nb / tb,
              "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
                      "and potentials; one CUDA graph with a concurrent branch per grid size"}
+    stand_in = None
+    if rank == 0:
+        stand_in = gpu_stand_in(dev, E_host, V, sim, plan, op)
     sur = None
     if rank == 0 and not args.no_surrogate:
         sur = surrogate_leg(dev)
@@ -498,6 +569,7 @@ def run_gb300(args):
                            "kernel_variant": tuned,
                            "single_field_loop": single, "single_field_loop_c128": single_c128,
                            "cnlse_1024_nonlocal": cnlse, "mixed_batch_164": mixed,
+                           "reference_gpu_stand_in": stand_in,
                            "surrogate_256": sur},
                 "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks}

@@ -205,8 +205,8 @@ class NLSE:
             lead = self._lead_shape(tuple(A.shape))
             nseg = int(np.prod(lead)) * self._comps if lead else self._comps
             sums = engine.power(src, nseg)
-            target = torch.from_numpy(np.ascontiguousarray(
-                self._norm_target(lead).reshape(-1))).to(dev)
+            target = torch.from_numpy(np.array(self._norm_target(lead), dtype=np.float64)
+                                      .reshape(-1)).to(dev)
             engine.normalize(src, A, nseg, sums, target, self._norm_coef())
         else:
             A.copy_(src)
