@@ -98,3 +98,42 @@ def test_3d_boxes_c128(NY, NX, NZ, precision):
     ref, _ = o.out_field(E, 3 * 2.5e-4, precision=precision)
     assert got.shape == (NY, NX, NZ)
     assert rel_l2(got, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+@pytest.mark.parametrize("omega", [None, 2e3])
+@pytest.mark.parametrize("NY,NX", [(8, 8), (16, 64), (64, 16), (256, 256), (128, 1024),
+                                   (1024, 1024)])
+def test_cnlse_geometry_c128(NY, NX, omega, precision):
+    out = []
+    for cls in (ng.CNLSE, orc.OracleCNLSE):
+        window = WINDOW if NY == NX else [WINDOW, WINDOW * NY / NX]
+        s = cls(ALPHA, 0.5, window, N2, -0.8e-9, None, 20e-3, NX=NX, NY=NY, Isat=ISAT,
+                omega=omega)
+        s.delta_z = DZ
+        s.power2 = 0.05
+        s.n22 = -1.2e-9
+        s.k2 = 2 * np.pi / 795e-9
+        s.V = (-1e-4 * np.exp(-(s.XX**2 + s.YY**2) / WAIST2**2)).astype(np.complex64)
+        E = np.array([np.exp(-(s.XX**2 + s.YY**2) / w**2) for w in (1.5e-3, 0.5e-3)])
+        out.append((s, E.astype(np.complex128)))
+    (p, E), (o, _) = out
+    got = p.out_field(E, STEPS * DZ, precision=precision, verbose=False)
+    ref, _ = o.out_field(E, STEPS * DZ, precision=precision)
+    assert got.shape == (2, NY, NX)
+    assert rel_l2(got, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("NX", [4, 64, 2048])
+def test_cnlse_1d_lengths_c128(NX):
+    out = []
+    for cls in (ng.CNLSE_1d, orc.OracleCNLSE_1d):
+        s = cls(ALPHA, POWER, WINDOW, N2, -1e-10, None, L, NX=NX, Isat=ISAT)
+        s.delta_z = DZ
+        s.power2 = 10e-3
+        E = np.array([np.exp(-s.X**2 / w**2) for w in (WAIST, WAIST / 2)])
+        out.append((s, E.astype(np.complex128)))
+    (p, E), (o, _) = out
+    got = p.out_field(E, STEPS * DZ, verbose=False)
+    ref, _ = o.out_field(E, STEPS * DZ)
+    assert rel_l2(got, ref) <= 1e-12
