@@ -140,9 +140,9 @@ int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nst
  * (its own plan, field and operator) runs its nsteps[i] split steps on a
  * branch of one CUDA graph, the branches concurrent, so the whole batched
  * z-loop is one graph launch (replayed when called again with the same
- * arguments; NLSE_RUN_GRAPH is implied).  The batch of SURVEY-style mixed
- * grids (e.g. 96 fields at 256^2, 48 at 512^2, 16 at 1024^2, 4 at 2048^2)
- * is four groups.  No reference counterpart as one call: the reference runs
+ * arguments; NLSE_RUN_GRAPH is implied).  A batch of mixed grids (e.g.
+ * 96 fields at 256^2, 48 at 512^2, 16 at 1024^2, 4 at 2048^2) is four
+ * groups.  No reference counterpart as one call: the reference runs
  * one out_field per NLSE instance.
  */
 typedef struct nlse_group_s* nlse_group;
