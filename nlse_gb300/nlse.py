@@ -38,6 +38,34 @@ def _host(x):
     return x
 
 
+def nonlinear_length(k: float, n2, power, w2: float):
+    """1 / (k |n2 * power / w2|), minimised over the broadcast of n2 and power
+    when either is an array (the default step of nlse.py:108-114 and
+    nlse_3d.py:105-111), without forming that broadcast: a per-field n2
+    (B, 1, 1) and power (B,) would make a (B, 1, B) array.  Every factor
+    enters through its absolute value and rounding is monotone, so the
+    minimum is the same expression evaluated at the largest |n2 * power|,
+    which each operand reaches after a reduction over the axes the other one
+    broadcasts along: the value is bit for bit the minimum of the array."""
+    if not (isinstance(n2, np.ndarray) or isinstance(power, np.ndarray)):
+        return 1 / (k * abs(n2 * power / w2))
+    # NumPy's absolute value keeps each operand's type, and a Python scalar
+    # stays a Python scalar (weak in NumPy's promotion, as in the product)
+    a = np.abs(n2) if isinstance(n2, (np.ndarray, np.generic)) else abs(n2)
+    b = np.abs(power) if isinstance(power, (np.ndarray, np.generic)) else abs(power)
+    if isinstance(a, np.ndarray) and isinstance(b, np.ndarray):
+        nd = max(a.ndim, b.ndim)
+        a = a.reshape((1,) * (nd - a.ndim) + a.shape)
+        b = b.reshape((1,) * (nd - b.ndim) + b.shape)
+        np.broadcast_shapes(a.shape, b.shape)  # incompatible shapes raise as the product would
+        for ax in range(nd):
+            if a.shape[ax] == 1 and b.shape[ax] > 1:
+                b = b.max(axis=ax, keepdims=True)
+            elif b.shape[ax] == 1 and a.shape[ax] > 1:
+                a = a.max(axis=ax, keepdims=True)
+    return (1 / (k * ((a * b) / w2))).min()
+
+
 def count_steps(z: float, delta_z) -> int:
     """Number of iterations of `while abs(z_prop) < z: z_prop += delta_z`.
 
@@ -109,10 +137,10 @@ class NLSE:
         else:
             self.window = list(window)
         # default step: 1/200 of the nonlinear length (nlse.py:108-114)
-        Dn = self.n2 * self.power / min(self.window) ** 2
-        z_nl = 1 / (self.k * abs(Dn))
-        if isinstance(z_nl, np.ndarray):
-            z_nl = float(z_nl.min())
+        z_nl = nonlinear_length(self.k, self.n2, self.power, min(self.window) ** 2)
+        if isinstance(self.n2, np.ndarray) or isinstance(self.power, np.ndarray):
+            if np.broadcast_shapes(np.shape(self.n2), np.shape(self.power)) != ():
+                z_nl = float(z_nl)  # the minimum of an array, as a Python float
         self.delta_z = 5e-3 * z_nl
         # float32 transverse grid, float64 step (nlse.py:116-131)
         self.X, self.delta_X = np.linspace(

@@ -116,14 +116,8 @@ def solve(inp: dict, steps: int | None = None, chunk: int = 2048) -> torch.Tenso
     for b0 in range(0, n, chunk):
         sl = slice(b0, min(n, b0 + chunk))
         B = sl.stop - sl.start
-        # constructed with scalars, then given the per-field arrays: the
-        # constructor's default step (overridden below) would otherwise form
-        # the (B, 1, B) broadcast of n2 (B, 1, 1) times power (B,), ~17 ms at
-        # B = 2048; out_field reads power and n2 from the attributes
-        sim = NLSE(ALPHA, float(inp["power"][sl][0]), WINDOW, float(inp["n2"][sl][0]), None, L,
+        sim = NLSE(ALPHA, inp["power"][sl], WINDOW, inp["n2"][sl].reshape(B, 1, 1), None, L,
                    NX=N, NY=N, Isat=ISAT)
-        sim.power = inp["power"][sl]
-        sim.n2 = inp["n2"][sl].reshape(B, 1, 1)
         sim.V = inp["V"][sl]
         if steps is None:
             sim.delta_z = DZ
