@@ -14,7 +14,7 @@ import numpy as np
 from scipy.constants import c, epsilon_0
 
 from . import engine
-from .nlse import NLSE, __BACKEND__
+from .nlse import NLSE, __BACKEND__, nonlinear_length
 
 
 class NLSE_3d(NLSE):
