@@ -164,8 +164,16 @@ class NLSE:
 
     @staticmethod
     def _k0_profile(nl_length: float, delta_X: float) -> np.ndarray:
-        """Normalised K0 Bessel nonlocal kernel of size (6d+1)^2 (nlse.py:143-153)."""
+        """Normalised K0 Bessel nonlocal kernel of size (6d+1)^2 (nlse.py:143-153).
+
+        With nl_length < delta_X, d = 0 and the kernel is NaN, as in the
+        reference (every field it enters becomes NaN); a RuntimeWarning says
+        so at construction instead of leaving it to the results."""
         d = nl_length // delta_X
+        if d == 0:
+            warnings.warn(f"nl_length = {nl_length:g} m is below the grid step {delta_X:g} m: "
+                          "the K0 nonlocal kernel is NaN (as in the reference); use nl_length "
+                          ">= the grid step or set nl_profile", RuntimeWarning, stacklevel=3)
         r = np.arange(-3 * d, 3 * d + 1)
         xx, yy = np.meshgrid(r, r)
         prof = special.kn(0, np.hypot(xx, yy) / d)
