@@ -265,6 +265,28 @@ def run_callbacks(R, name, N, dtype, precision, batch=None, adapt_every=0, every
          power=np.asarray(power), precision=np.array(precision))
 
 
+def run_cnlse1d(R, name, dtype, precision):
+    sim = R.CNLSE_1d(ALPHA, POWER, WINDOW, N2, -1e-10, None, L, NX=128, Isat=ISAT,
+                     backend="GPU")
+    sim.delta_z = 5e-5
+    sim.power2 = 10e-3
+    E = np.array([gauss(sim.X, 0), gauss(sim.X, 0, WAIST / 3)]).astype(dtype)
+    out = sim.out_field(E, L, precision=precision, verbose=False)
+    save(name, E_in=E, out=out, meta=np.array([128, 5e-5, L]))
+
+
+def run_gpe(R, name, dtype, precision):
+    from scipy.constants import atomic_mass
+
+    sim = R.GPE(gamma=0.5, N=2e5, window=40e-6, g=1e3 / 2e5 * 1e-12, V=None,
+                m=87 * atomic_mass, NX=32, NY=32, sat=1e15, backend="GPU")
+    sim.delta_z = 1e-5
+    sim.delta_t = 1e-5
+    E = np.exp(-(sim.XX**2 + sim.YY**2) / (5e-6) ** 2).astype(dtype)
+    out = sim.out_field(E, 2e-4, precision=precision, verbose=False)
+    save(name, E_in=E, out=out, meta=np.array([32, 1e-5, 2e-4]))
+
+
 def main() -> None:
     import os
     import tempfile
@@ -337,25 +359,11 @@ def main() -> None:
         save(f"cnlse_{tag}", E_in=E, V=sim.V, out=out,
              meta=np.array([32, 5e-5, 20e-3, -1 if omega is None else omega]))
 
-    # CNLSE_1d
-    sim = R.CNLSE_1d(ALPHA, POWER, WINDOW, N2, -1e-10, None, L, NX=128, Isat=ISAT,
-                     backend="GPU")
-    sim.delta_z = 5e-5
-    sim.power2 = 10e-3
-    E = np.array([gauss(sim.X, 0), gauss(sim.X, 0, WAIST / 3)]).astype(np.complex64)
-    out = sim.out_field(E, L, precision="single", verbose=False)
-    save("cnlse1d_c64_single", E_in=E, out=out, meta=np.array([128, 5e-5, L]))
-
-    # GPE
-    from scipy.constants import atomic_mass
-
-    sim = R.GPE(gamma=0.5, N=2e5, window=40e-6, g=1e3 / 2e5 * 1e-12, V=None,
-                m=87 * atomic_mass, NX=32, NY=32, sat=1e15, backend="GPU")
-    sim.delta_z = 1e-5
-    sim.delta_t = 1e-5
-    E = np.exp(-(sim.XX**2 + sim.YY**2) / (5e-6) ** 2).astype(np.complex64)
-    out = sim.out_field(E, 2e-4, precision="single", verbose=False)
-    save("gpe_c64_single", E_in=E, out=out, meta=np.array([32, 1e-5, 2e-4]))
+    # CNLSE_1d and GPE, complex64 "single" and complex128 "double"
+    run_cnlse1d(R, "cnlse1d_c64_single", np.complex64, "single")
+    run_cnlse1d(R, "cnlse1d_c128_double", np.complex128, "double")
+    run_gpe(R, "gpe_c64_single", np.complex64, "single")
+    run_gpe(R, "gpe_c128_double", np.complex128, "double")
 
     # DDGPE with the pump as callback 0 (and the branch-specific arguments)
     for prec, with_v, tag in (("single", False, "single_noV"), ("single", True, "single_V"),

@@ -81,7 +81,7 @@ def run(name: str, kind: str, upcast: bool = False):
         sim = C["CNLSE_1d"](ALPHA, POWER, WINDOW, N2, -1e-10, None, L, NX=128, Isat=ISAT)
         sim.delta_z = 5e-5
         sim.power2 = 10e-3
-        return _out(kind, sim, E, L, "single")
+        return _out(kind, sim, E, L, "double" if "double" in name else "single")
     if name.startswith("cnlse"):
         omega = float(f["meta"][3])
         sim = C["CNLSE"](ALPHA, 0.5, WINDOW, N2, -0.8e-9, None, 20e-3, NX=32, NY=32, Isat=ISAT,
@@ -97,7 +97,7 @@ def run(name: str, kind: str, upcast: bool = False):
                        m=87 * atomic_mass, NX=32, NY=32, sat=1e15)
         sim.delta_z = 1e-5
         sim.delta_t = 1e-5
-        return _out(kind, sim, E, 2e-4, "single")
+        return _out(kind, sim, E, 2e-4, "double" if "double" in name else "single")
     if name.startswith("ddgpe"):
         h = 0.654
         sim = C["DDGPE"](gamma=0.07 / h, power=1.0, window=64.0, g=1e-2 / h, omega=5.07 / h,
