@@ -170,3 +170,37 @@ def test_cnlse_parameter_block():
     assert P[0, 13] == cn.k2 / 2
     assert np.isclose(P[0, 15], np.sin(1e3 * cn.delta_z))
     assert cn._rabi_enabled("single") and not cn._rabi_enabled("double")
+
+
+def _arg_error_cases(lib):
+    z = ct.c_void_p(None)
+    fake = ct.c_void_p(16)  # never dereferenced: every call below fails its argument check first
+    return [
+        ("add_noise null field", lambda: lib.nlse_add_noise(z, 0, 1, 16, 0.1, 0.1, 1, 0, z)),
+        ("add_noise bad dtype", lambda: lib.nlse_add_noise(fake, 7, 1, 16, 0.1, 0.1, 1, 0, z)),
+        ("add_noise negative step",
+         lambda: lib.nlse_add_noise(fake, 0, 1, 16, 0.1, 0.1, 1, -1, z)),
+        ("delta_n null coef", lambda: lib.nlse_delta_n(fake, 0, 1, 16, z, fake, 0, fake, z)),
+        ("delta_n bad flags", lambda: lib.nlse_delta_n(fake, 0, 1, 16, fake, fake, 4, fake, z)),
+        ("delta_n empty", lambda: lib.nlse_delta_n(fake, 0, 0, 16, fake, fake, 0, fake, z)),
+        ("delta_n_max bad dtype",
+         lambda: lib.nlse_delta_n_max(fake, 3, 1, 16, fake, fake, 1.0, 1.0, 0, fake, z)),
+        ("wait_selftest zero limit", lambda: lib.nlse_wait_selftest(fake, fake, 0, z)),
+        ("wait_selftest over 1 s", lambda: lib.nlse_wait_selftest(fake, fake, 2_000_000_000, z)),
+        ("set_kernels null plan", lambda: lib.nlse_plan_set_kernels(z, 1, 1)),
+        ("propagate null plan", lambda: lib.nlse_propagate(z, fake, None, 1, 0, 0, z)),
+        ("pass null plan", lambda: lib.nlse_pass(z, fake, None, 0, 0, z)),
+        ("normalize null", lambda: lib.nlse_normalize(z, z, 0, 1, 1, z, z, 1.0, z)),
+        ("square_mod bad dtype", lambda: lib.nlse_square_mod(fake, fake, 9, 16, z)),
+        ("fno_lift_rows empty batch",
+         lambda: lib.nlse_fno_lift_rows(0, fake, fake, fake, fake, fake, fake, z)),
+        ("fno_mix empty batch", lambda: lib.nlse_fno_mix(0, fake, fake, fake, fake, z)),
+        ("fno_loss empty batch", lambda: lib.nlse_fno_loss(0, fake, fake, fake, fake, fake, z)),
+    ]
+
+
+def test_entry_points_reject_bad_arguments_before_any_device_work(lib):
+    for name, call in _arg_error_cases(lib):
+        rc = call()
+        assert rc == _lib.ERR_ARG, (name, rc, _lib.last_error())
+        assert _lib.last_error(), name
