@@ -287,6 +287,23 @@ def run_gpe(R, name, dtype, precision):
     save(name, E_in=E, out=out, meta=np.array([32, 1e-5, 2e-4]))
 
 
+def run_cnlse_nonlocal(R, name, dtype, precision):
+    """CNLSE with a Gaussian nonlocal kernel (the 1024^2 coupled configuration's
+    physics at 64^2; the kernel set through nl_profile, sigma 100 um)."""
+    sim = R.CNLSE(ALPHA, 0.5, WINDOW, N2, -0.8e-9, None, 20e-3, NX=64, NY=64, Isat=ISAT,
+                  nl_length=100e-6, backend="GPU")
+    r = np.arange(-10, 11) * sim.delta_X
+    kern = np.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * (100e-6) ** 2))
+    kern = kern / kern.sum()
+    sim.nl_profile = kern
+    sim.delta_z = 5e-5
+    sim.power2 = 0.05
+    sim.n22 = -1.6e-9
+    E = np.array([gauss(sim.XX, sim.YY, 1.5e-3), gauss(sim.XX, sim.YY, 0.5e-3)]).astype(dtype)
+    out = sim.out_field(E, 2e-3, precision=precision, verbose=False)
+    save(name, E_in=E, out=out, nl_profile=kern, meta=np.array([64, 5e-5, 2e-3]))
+
+
 def main() -> None:
     import os
     import tempfile
@@ -364,6 +381,8 @@ def main() -> None:
     run_cnlse1d(R, "cnlse1d_c128_double", np.complex128, "double")
     run_gpe(R, "gpe_c64_single", np.complex64, "single")
     run_gpe(R, "gpe_c128_double", np.complex128, "double")
+    run_cnlse_nonlocal(R, "cnlsenl_c64_single", np.complex64, "single")
+    run_cnlse_nonlocal(R, "cnlsenl_c128_double", np.complex128, "double")
 
     # DDGPE with the pump as callback 0 (and the branch-specific arguments)
     for prec, with_v, tag in (("single", False, "single_noV"), ("single", True, "single_V"),

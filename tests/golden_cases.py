@@ -77,6 +77,14 @@ def run(name: str, kind: str, upcast: bool = False):
                            n2=N2, D0=1e-16, vg=3e7, V=None, L=L, NX=16, NY=16, NZ=8, Isat=ISAT)
         sim.delta_z = 2.5e-4
         return _out(kind, sim, E, L, "double" if "double" in name else "single")
+    if name.startswith("cnlsenl"):
+        sim = C["CNLSE"](ALPHA, 0.5, WINDOW, N2, -0.8e-9, None, 20e-3, NX=64, NY=64, Isat=ISAT,
+                         nl_length=100e-6)
+        sim.nl_profile = f["nl_profile"].copy()
+        sim.delta_z = 5e-5
+        sim.power2 = 0.05
+        sim.n22 = -1.6e-9
+        return _out(kind, sim, E, 2e-3, "double" if "double" in name else "single")
     if name.startswith("cnlse1d"):
         sim = C["CNLSE_1d"](ALPHA, POWER, WINDOW, N2, -1e-10, None, L, NX=128, Isat=ISAT)
         sim.delta_z = 5e-5
