@@ -204,3 +204,22 @@ def test_entry_points_reject_bad_arguments_before_any_device_work(lib):
         rc = call()
         assert rc == _lib.ERR_ARG, (name, rc, _lib.last_error())
         assert _lib.last_error(), name
+
+
+def _declared_arities():
+    """Parameter count of every nlse_* prototype in include/*.h."""
+    text = "\n".join(h.read_text() for h in sorted(HEADER.parent.glob("*.h")))
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)  # comments out
+    out = {}
+    for m in re.finditer(r"(?:int|size_t|const char\s*\*|void)\s+(nlse_\w+)\s*\(([^)]*)\)\s*;",
+                         text):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    ar = _declared_arities()
+    assert len(ar) >= 10
+    for name, _, argtypes in _lib.SIGNATURES:
+        assert ar[name] == len(argtypes), (name, ar[name], len(argtypes))
