@@ -223,3 +223,34 @@ def test_ctypes_signatures_match_the_header_prototypes():
     assert len(ar) >= 10
     for name, _, argtypes in _lib.SIGNATURES:
         assert ar[name] == len(argtypes), (name, ar[name], len(argtypes))
+
+
+def test_ctypes_structs_have_the_c_layout(tmp_path):
+    """nlse_desc and nlse_operator as gcc lays them out (include/nlse_gb300.h)
+    against the ctypes structures the Python host passes."""
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"nlse_desc": _lib.Desc, "nlse_operator": _lib.Operator}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "nlse_gb300.h"',
+             "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{HEADER.parent}", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.splitlines():
+        cname, fname, v = line.split()
+        got[(cname, fname)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ct.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
