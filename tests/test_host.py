@@ -254,3 +254,15 @@ def test_ctypes_structs_have_the_c_layout(tmp_path):
         assert got[(cname, "sizeof")] == ct.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_surrogate_constants_match_the_header():
+    """nlse_gb300.fno's sizes against the #defines of include/nlse_fno.h."""
+    from nlse_gb300 import fno
+
+    text = (HEADER.parent / "nlse_fno.h").read_text()
+    d = {k: int(v) for k, v in re.findall(r"#define NLSE_FNO_(\w+)\s+(\d+)", text)}
+    assert (fno.N, fno.C, fno.NM) == (d["N"], d["C"], d["MODES"])
+    assert (fno.PART_LAYER, fno.PART_PROJ, fno.PART_LIFT) == (
+        d["PART_LAYER"], d["PART_PROJ"], d["PART_LIFT"])
+    assert d["PART_LAYER"] == d["C"] * d["C"] + d["C"] and d["PART_PROJ"] == 2 * d["C"] + 2
