@@ -120,6 +120,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-surrogate", action="store_true",
                     help="leave out the surrogate-vs-solver leg (about a minute)")
+    ap.add_argument("--network-only", type=int, default=0, metavar="FIELDS",
+                    help="only time the surrogate network's inference on FIELDS random "
+                         "256^2 inputs (--steps passes after one warm-up; for profiling)")
     return ap.parse_args()
 
 
@@ -578,9 +581,39 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def network_only(args):
+    """Inference throughput of an initialised surrogate network on random inputs."""
+    import torch
+
+    from nlse_gb300 import _build
+    from nlse_gb300.fno import FNO, N as FN
+
+    _build.build()
+    nf = args.network_only
+    net = FNO("cuda")
+    g = torch.Generator(device="cuda").manual_seed(0)
+    xin = torch.randn((nf, FN, FN, 3), device="cuda", generator=g) * 0.3
+    xs = torch.randn((nf, 2), device="cuda", generator=g)
+    net.predict(xin, xs, chunk=nf)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(args.steps):
+        net.predict(xin, xs, chunk=nf)
+    b.record()
+    torch.cuda.synchronize()
+    net.check_status()
+    t = a.elapsed_time(b) / 1e3 / args.steps
+    print(json.dumps({"surrogate_network_only": {"fields": nf, "passes": args.steps,
+                                                 "ms_per_pass": round(t * 1e3, 3),
+                                                 "fields_per_s": round(nf / t, 1)}}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.network_only:
+        network_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

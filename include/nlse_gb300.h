@@ -239,7 +239,9 @@ int nlse_power(const void* A, int32_t dtype, int64_t nseg, int64_t seg_len, doub
  *     requests return NLSE_ERR_ARG with the numbers in nlse_last_error();
  *   - the first call on a device looks the array's device address up
  *     (cudaGetSymbolAddress), so make that first call before any stream
- *     capture on that device;
+ *     capture on that device; the address is kept per device and context,
+ *     so after a cudaDeviceReset the next call looks it up again (make
+ *     that call outside a capture too);
  *   - all calls share the array: calls whose kernels overlap on the GPU
  *     (different streams without ordering between them) race and may
  *     return wrong sums; order them on one stream.

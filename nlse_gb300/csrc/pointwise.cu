@@ -275,9 +275,29 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
 int64_t noalloc_partials_max() { return kNoAllocPartials; }
 
 // Device address of the array on the current device, looked up once per
-// device (the name is only a host-side stand-in in host code).
+// device and context (the name is only a host-side stand-in in host code).
+// The context is part of the key: after cudaDeviceReset the module is
+// loaded again and the array may sit at another address.
 static std::mutex g_noalloc_mu;
 static double* g_noalloc_ptr[64] = {};
+static void* g_noalloc_ctx[64] = {};
+
+// The calling thread's current driver context (null if it cannot be read).
+static void* current_context() {
+  using GetFn = int (*)(void**);
+  static GetFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<GetFn>(f);
+  }();
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 cudaError_t launch_power_noalloc(int dtype, const void* A, int64_t nseg, int64_t seg_len,
                                  double* out, cudaStream_t s) {
@@ -288,11 +308,13 @@ cudaError_t launch_power_noalloc(int dtype, const void* A, int64_t nseg, int64_t
   double* partial = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    void* ctx = current_context();
+    if (!g_noalloc_ptr[dev] || !ctx || ctx != g_noalloc_ctx[dev]) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_partials);
       if (e != cudaSuccess) return e;
       g_noalloc_ptr[dev] = static_cast<double*>(p);
+      g_noalloc_ctx[dev] = ctx;
     }
     partial = g_noalloc_ptr[dev];
   }

@@ -249,32 +249,3 @@ class FNO:
                                           self.steps, wd, stream_handle(self.dev)), "fno adam")
         self.pack()
         return loss
-
-
-def _main() -> None:
-    """Inference throughput of an initialised network on random inputs (fields/s)."""
-    import argparse
-
-    ap = argparse.ArgumentParser(description="surrogate network inference throughput")
-    ap.add_argument("--fields", type=int, default=512)
-    ap.add_argument("--reps", type=int, default=3)
-    args = ap.parse_args()
-    net = FNO("cuda")
-    g = torch.Generator(device="cuda").manual_seed(0)
-    xin = torch.randn((args.fields, N, N, 3), device="cuda", generator=g) * 0.3
-    xs = torch.randn((args.fields, 2), device="cuda", generator=g)
-    net.predict(xin, xs, chunk=args.fields)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    a.record()
-    for _ in range(args.reps):
-        net.predict(xin, xs, chunk=args.fields)
-    b.record()
-    torch.cuda.synchronize()
-    net.check_status()
-    t = a.elapsed_time(b) / 1e3 / args.reps
-    print(f"{args.fields} fields in {t * 1e3:.3f} ms: {args.fields / t:.1f} fields/s")
-
-
-if __name__ == "__main__":
-    _main()

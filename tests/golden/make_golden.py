@@ -1,8 +1,8 @@
 """Generate the golden fixtures by running the reference package itself.
 
-Runs Quantum-Optics-LKB/NLSE v2.3.0 (read from /root/reference, the one
-place this path is named) unmodified, with import stand-ins for the
-third-party modules that are absent here:
+Runs Quantum-Optics-LKB/NLSE v2.3.0 unmodified, from a source checkout
+given on the command line or in NLSE_REFERENCE_ROOT, with import stand-ins
+for the third-party modules that are absent here:
 
   cupy           NumPy arrays (an ndarray subclass with .get()), cp.fuse = identity
   cupyx.scipy.signal.oaconvolve -> scipy.signal.oaconvolve
@@ -16,7 +16,8 @@ So the fixtures hold the reference's own split-step/out_field arithmetic in
 NumPy semantics; only the FFT implementation is substituted.  Output:
 tests/golden/*.npz (inputs, parameters and outputs of each case).
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
+       (or NLSE_REFERENCE_ROOT=REFERENCE_ROOT python tests/golden/make_golden.py)
 """
 
 from __future__ import annotations
@@ -30,7 +31,14 @@ import scipy.fft as sfft
 import scipy.signal as ssig
 
 OUT = Path(__file__).resolve().parent
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+def _reference_root() -> Path:
+    import os
+
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NLSE_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT (the NLSE source checkout; "
+                         "or set NLSE_REFERENCE_ROOT)")
+    return Path(root)
 
 
 # ---------------------------------------------------------------------------
@@ -157,9 +165,9 @@ def _install_shims() -> None:
     sys.modules["pyvkfft.cuda"] = pvc
 
 
-def load_reference():
+def load_reference(root: Path | None = None):
     _install_shims()
-    sys.path.insert(0, str(REF))
+    sys.path.insert(0, str(root if root is not None else _reference_root()))
     import NLSE  # noqa: N811  (the reference package)
 
     return NLSE
@@ -309,9 +317,10 @@ def main() -> None:
     import tempfile
 
     # the reference's CPU path writes an FFTW wisdom file into the working directory
+    ref = _reference_root().resolve()
     os.chdir(tempfile.mkdtemp(prefix="nlse_golden_"))
-    R = load_reference()
-    print(f"reference NLSE {R.__version__} from {REF}")
+    R = load_reference(ref)
+    print(f"reference NLSE {R.__version__} from {ref}")
     # NLSE 2-D: the benchmark physics at 64^2
     run_nlse2d(R, "nlse2d_c64_single", 64, np.complex64, "single")
     run_nlse2d(R, "nlse2d_c128_double", 64, np.complex128, "double")

@@ -196,6 +196,11 @@ def _arg_error_cases(lib):
          lambda: lib.nlse_fno_lift_rows(0, fake, fake, fake, fake, fake, fake, z)),
         ("fno_mix empty batch", lambda: lib.nlse_fno_mix(0, fake, fake, fake, fake, z)),
         ("fno_loss empty batch", lambda: lib.nlse_fno_loss(0, fake, fake, fake, fake, fake, z)),
+        # 32769 segments of 8193 elements need 65,538 partial sums: two over the static array
+        ("power_noalloc over capacity",
+         lambda: lib.nlse_power_noalloc(fake, 0, 32769, 8193, fake, z)),
+        ("power_noalloc 1024 partials x 65 segments",
+         lambda: lib.nlse_power_noalloc(fake, 0, 65, 1024 * 8192, fake, z)),
     ]
 
 
