@@ -163,6 +163,34 @@ int nlse_plan_set_kernels(nlse_plan plan, int32_t rows_tma, int32_t cols_tma);
 int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
                           int32_t* rows_tma_ok, int32_t* cols_tma_ok);
 
+/* The same choice with every variant and launch shape, as codes:
+ *   rows: NLSE_ROWS_LINE (one CTA per line), NLSE_ROWS_TMA (TMA-fed
+ *         persistent), NLSE_ROWS_PAIR (TMA-fed persistent, two lines per
+ *         thread in packed FP32: one-component complex64 fields, rows of
+ *         64..4096 points);
+ *   cols: NLSE_COLS_TILE (one CTA per tile), NLSE_COLS_TMA (persistent bulk-
+ *         copy ring), NLSE_COLS_PAIR (the ring with two columns per thread in
+ *         packed FP32: complex64, columns of 64..2048 points).
+ * rows_ctas_per_sm / cols_ctas_per_sm cap the persistent passes' CTAs per SM
+ * (0: as many as fit), which sets their grid (SMs x CTAs per SM).  A launch
+ * the chosen variant cannot serve (two components, Rabi or pump terms, a
+ * complex128 propagator, an external |A|^2) runs the TMA variant instead.
+ * get returns the current choice and bit masks of the available variants
+ * (bit v set: variant code v).  The plan's default is the pair variants
+ * where available, else the TMA ones.  No reference counterpart (the
+ * reference's VkFFTApp(tune=True) tunes its FFT plan, NLSE/nlse.py:216);
+ * nlse_gb300.autotune searches these. */
+#define NLSE_ROWS_LINE 0
+#define NLSE_ROWS_TMA 1
+#define NLSE_ROWS_PAIR 2
+#define NLSE_COLS_TILE 0
+#define NLSE_COLS_TMA 1
+#define NLSE_COLS_PAIR 2
+int nlse_plan_set_variant(nlse_plan plan, int32_t rows, int32_t cols, int32_t rows_ctas_per_sm,
+                          int32_t cols_ctas_per_sm);
+int nlse_plan_get_variant(nlse_plan plan, int32_t* rows, int32_t* cols, int32_t* rows_ctas_per_sm,
+                          int32_t* cols_ctas_per_sm, uint32_t* rows_avail, uint32_t* cols_avail);
+
 /*
  * Nonlocal response (the reference's oaconvolve(|A|^2, nl_profile, "same")
  * over the transform axes, NLSE/nlse.py:143-155, 406-408, 444-447 and the

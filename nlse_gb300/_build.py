@@ -31,6 +31,9 @@ SOURCES = [
     "rows_f64_c2.cu",
     "cols_f32.cu",
     "cols_f64.cu",
+    "rows_pair_mid.cu",
+    "rows_pair_last.cu",
+    "cols_pair.cu",
     "fno.cu",
 ]
 

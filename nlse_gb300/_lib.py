@@ -17,6 +17,9 @@ NLSE_C128 = 1
 NLSE_RUN_GRAPH = 1
 NLSE_PARAM_STRIDE = 40
 PASS_FORWARD, PASS_LINEAR, PASS_INV_NL_FWD, PASS_INV_NL = 0, 1, 2, 3
+# kernel variants of the 2-D passes (nlse_plan_set_variant)
+ROWS_LINE, ROWS_TMA, ROWS_PAIR = 0, 1, 2
+COLS_TILE, COLS_TMA, COLS_PAIR = 0, 1, 2
 DN_COEF_F64, DN_ISAT_F64 = 1, 2
 
 OK = 0
@@ -68,6 +71,10 @@ SIGNATURES = [
     ("nlse_plan_set_nonlocal", ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int64]),
     ("nlse_plan_set_kernels", ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32]),
     ("nlse_plan_get_kernels", ct.c_int, [ct.c_void_p] + [ct.POINTER(ct.c_int32)] * 4),
+    ("nlse_plan_set_variant", ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32,
+                                         ct.c_int32]),
+    ("nlse_plan_get_variant", ct.c_int, [ct.c_void_p] + [ct.POINTER(ct.c_int32)] * 4
+     + [ct.POINTER(ct.c_uint32)] * 2),
     ("nlse_group_create", ct.c_int, [ct.POINTER(ct.c_void_p)]),
     ("nlse_group_destroy", ct.c_int, [ct.c_void_p]),
     (

@@ -164,6 +164,10 @@ struct nlse_plan_s {
   bool rows_tma = false;        // use the TMA-fed inverse row passes
   bool cols_tma_ok = true;      // the TMA column pass is available (not disabled)
   bool rows_tma_ok = false;     // tensor map of S encoded: the TMA row passes are available
+  int rows_var = NLSE_ROWS_LINE;  // inverse row pass variant (NLSE_ROWS_*)
+  int cols_var = NLSE_COLS_TILE;  // column pass variant (NLSE_COLS_*)
+  int rows_cap = 0, cols_cap = 0; // CTAs per SM of the persistent passes (0: all that fit)
+  uint32_t rows_avail = 1u << NLSE_ROWS_LINE, cols_avail = 1u << NLSE_COLS_TILE;
   uint64_t kgen = 0;            // kernel-variant generation (part of every graph key)
   CUtensorMap tmS;              // S as {2W scalars, NY, NX/W, slabs}, box = one row (<= 256 runs)
   // nonlocal response: zero-padded grid (py x px), its scratch and FFT plan
@@ -174,8 +178,31 @@ struct nlse_plan_s {
 
 namespace {
 
+// The pair row pass serves this launch: complex64 one-component field on
+// the blocked buffer through the tensor map, no Rabi, pump or external |A|^2.
+bool rows_pair_fits(const nlse_plan_s* p, int mode, const StepArgs& a) {
+  return p->rows_var == NLSE_ROWS_PAIR && p->d.dtype == NLSE_C64 && a.comps == 1 &&
+         (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (a.flags & F_IN_BLK) && a.tmap &&
+         a.tma_grid > 0 && !(a.flags & (F_RABI | F_PUMP | F_PROBE | F_ASQ_EXT)) &&
+         (!(a.flags & F_HAS_V) || (a.flags & F_V_F32)) && a.nq % 2 == 0 &&
+         a.nq < (int64_t(1) << 31);
+}
+
 cudaError_t rows(const nlse_plan_s* p, int mode, int log2n, const StepArgs& a, cudaStream_t s,
                  bool prep = false) {
+  if (prep && p->d.dtype == NLSE_C64 && a.comps == 1 &&
+      (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (p->rows_avail >> NLSE_ROWS_PAIR & 1)) {
+    const cudaError_t e = launch_rows_pair(mode, log2n, a, false, s, true, 0);
+    if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+  }
+  if (!prep && rows_pair_fits(p, mode, a)) {
+    // the potential row is shared by both lines of every pair when one real
+    // potential serves an even number of fields (lines are field-fastest)
+    const bool vshared = (a.flags & F_HAS_V) && !(a.flags & F_V_COMPLEX) && a.v_fstride == 0 &&
+                         p->d.nfields % 2 == 0;
+    const cudaError_t e = launch_rows_pair(mode, log2n, a, vshared, s, false, p->rows_cap);
+    if (e != cudaErrorNotSupported) return e;
+  }
   if (p->d.dtype == NLSE_C64)
     return a.comps == 1 ? launch_rows_f32_c1(mode, log2n, a, s, prep)
                         : launch_rows_f32_c2(mode, log2n, a, s, prep);
@@ -191,6 +218,16 @@ cudaError_t cols(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a, cu
 
 cudaError_t cols_blk(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a, cudaStream_t s,
                      bool prep = false) {
+  if (p->d.dtype == NLSE_C64 && mode == COL_FWD_PROP_INV) {
+    if (prep && (p->cols_avail >> NLSE_COLS_PAIR & 1)) {
+      const cudaError_t e = launch_cols_pair(log2n, a, s, true, 0);
+      if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+    }
+    if (!prep && p->cols_var == NLSE_COLS_PAIR && a.tma_grid > 0 && !(a.flags & F_PROP_C128)) {
+      const cudaError_t e = launch_cols_pair(log2n, a, s, false, p->cols_cap);
+      if (e != cudaErrorNotSupported) return e;
+    }
+  }
   if (p->d.dtype == NLSE_C64) return launch_cols_blk_f32(mode, log2n, a, s, prep);
   return launch_cols_blk_f64(mode, log2n, a, s, prep);
 }
@@ -226,6 +263,7 @@ ColArgs col_blk_args(const nlse_plan_s* p, const nlse_operator* op) {
   c.nblocks = c.ncb * d.nfields * d.comps;
   c.status = p->status;
   c.tma_grid = p->cols_tma ? p->nsm : 0;
+  c.cap_per_sm = p->cols_cap;
   return c;
 }
 
@@ -288,6 +326,7 @@ StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
   a.status = p->status;
   a.tma_grid = p->rows_tma ? p->nsm : 0;
   a.tmap = p->rows_tma ? &p->tmS : nullptr;
+  a.cap_per_sm = p->rows_cap;
   const int64_t n = d.shape[d.ndim - 1];
   a.lines_per_comp = p->pix / n;
   a.nq = d.nfields * a.lines_per_comp;
@@ -646,6 +685,23 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     const int64_t nb = d.shape[1] / blk_width(p);
     if (rc == NLSE_OK && want && (nb <= 256 || nb % 256 == 0) && d.nfields * d.comps < (1ll << 31))
       p->rows_tma = p->rows_tma_ok = encode_tmap_S(&p->tmS, p->S, d, p->pix);
+    // variants: TMA row passes with the tensor map; pair passes (packed FP32,
+    // two lines per thread) for one-component complex64 fields of 64 to 4096
+    // points per row and 64 to 2048 per column, unless NLSE_PAIR=0
+    const char* penv = getenv("NLSE_PAIR");
+    const bool pair = !(penv && penv[0] == '0') && d.dtype == NLSE_C64 && d.comps == 1;
+    if (p->rows_tma_ok) p->rows_avail |= 1u << NLSE_ROWS_TMA;
+    if (p->rows_tma_ok && pair && p->lg[1] >= 6 && p->lg[1] <= 12)
+      p->rows_avail |= 1u << NLSE_ROWS_PAIR;
+    if (p->cols_tma_ok) p->cols_avail |= 1u << NLSE_COLS_TMA;
+    if (p->cols_tma_ok && pair && p->lg[0] >= 6 && p->lg[0] <= 11)
+      p->cols_avail |= 1u << NLSE_COLS_PAIR;
+    p->rows_var = (p->rows_avail >> NLSE_ROWS_PAIR & 1) ? NLSE_ROWS_PAIR
+                  : p->rows_tma                          ? NLSE_ROWS_TMA
+                                                         : NLSE_ROWS_LINE;
+    p->cols_var = (p->cols_avail >> NLSE_COLS_PAIR & 1) ? NLSE_COLS_PAIR
+                  : p->cols_tma                          ? NLSE_COLS_TMA
+                                                         : NLSE_COLS_TILE;
   }
   if (rc == NLSE_OK && p->fft_ok) rc = prepare_kernels(p);
   if (rc == NLSE_OK) {
@@ -860,6 +916,44 @@ int nlse_pass(nlse_plan p, void* A, const nlse_operator* op, int32_t pass, int64
   return enqueue_pass(p, A, op, pass, step, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int nlse_plan_set_variant(nlse_plan p, int32_t rows, int32_t cols, int32_t rows_ctas_per_sm,
+                          int32_t cols_ctas_per_sm) {
+  g_err.clear();
+  if (!p) return fail(NLSE_ERR_ARG, "null plan");
+  if (rows < 0 || rows > 2 || cols < 0 || cols > 2 || rows_ctas_per_sm < 0 ||
+      cols_ctas_per_sm < 0 || rows_ctas_per_sm > 32 || cols_ctas_per_sm > 32)
+    return fail(NLSE_ERR_ARG, "variant codes 0..2, CTAs per SM 0..32");
+  if (!(p->rows_avail >> rows & 1))
+    return fail(NLSE_ERR_UNSUPPORTED, "row pass variant %d is not available for this plan", rows);
+  if (!(p->cols_avail >> cols & 1))
+    return fail(NLSE_ERR_UNSUPPORTED, "column pass variant %d is not available for this plan", cols);
+  if (p->rows_var != rows || p->cols_var != cols || p->rows_cap != rows_ctas_per_sm ||
+      p->cols_cap != cols_ctas_per_sm) {
+    p->rows_var = rows;
+    p->cols_var = cols;
+    p->rows_tma = rows != NLSE_ROWS_LINE;
+    p->cols_tma = cols != NLSE_COLS_TILE;
+    p->rows_cap = rows_ctas_per_sm;
+    p->cols_cap = cols_ctas_per_sm;
+    ++p->kgen;  // captured graphs hold the old kernels
+  }
+  return NLSE_OK;
+}
+
+int nlse_plan_get_variant(nlse_plan p, int32_t* rows, int32_t* cols, int32_t* rows_ctas_per_sm,
+                          int32_t* cols_ctas_per_sm, uint32_t* rows_avail, uint32_t* cols_avail) {
+  g_err.clear();
+  if (!p || !rows || !cols || !rows_ctas_per_sm || !cols_ctas_per_sm || !rows_avail || !cols_avail)
+    return fail(NLSE_ERR_ARG, "null argument");
+  *rows = p->rows_var;
+  *cols = p->cols_var;
+  *rows_ctas_per_sm = p->rows_cap;
+  *cols_ctas_per_sm = p->cols_cap;
+  *rows_avail = p->rows_avail;
+  *cols_avail = p->cols_avail;
+  return NLSE_OK;
+}
+
 int nlse_plan_set_kernels(nlse_plan p, int32_t rows_tma, int32_t cols_tma) {
   g_err.clear();
   if (!p) return fail(NLSE_ERR_ARG, "null plan");
@@ -867,12 +961,8 @@ int nlse_plan_set_kernels(nlse_plan p, int32_t rows_tma, int32_t cols_tma) {
     return fail(NLSE_ERR_UNSUPPORTED, "this plan has no TMA row pass (geometry or disabled)");
   if (cols_tma && !p->cols_tma_ok)
     return fail(NLSE_ERR_UNSUPPORTED, "the TMA column pass is disabled for this plan");
-  if (p->rows_tma != (rows_tma != 0) || p->cols_tma != (cols_tma != 0)) {
-    p->rows_tma = rows_tma != 0;
-    p->cols_tma = cols_tma != 0;
-    ++p->kgen;  // captured graphs hold the old kernels
-  }
-  return NLSE_OK;
+  return nlse_plan_set_variant(p, rows_tma ? NLSE_ROWS_TMA : NLSE_ROWS_LINE,
+                               cols_tma ? NLSE_COLS_TMA : NLSE_COLS_TILE, 0, 0);
 }
 
 int nlse_plan_get_kernels(nlse_plan p, int32_t* rows_tma, int32_t* cols_tma,

@@ -40,6 +40,7 @@ static cudaError_t rows_tma_n(const StepArgs& a, cudaStream_t s, bool prep, bool
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
+    if (a.cap_per_sm > 0 && a.cap_per_sm < per_sm) per_sm = a.cap_per_sm;
     const int64_t groups = (a.nq + LPC - 1) / LPC;
     int64_t g = (int64_t)a.tma_grid * per_sm;
     if (g > groups) g = groups;
@@ -172,6 +173,7 @@ static cudaError_t cols_blk_tma_n(const ColArgs& a, cudaStream_t s, bool prep, i
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
+    if (a.cap_per_sm > 0 && a.cap_per_sm < per_sm) per_sm = a.cap_per_sm;
     int64_t g = (int64_t)grid * per_sm;
     if (g > a.nblocks) g = a.nblocks;
     kern<<<(unsigned)g, THREADS, smem, s>>>(a);

@@ -23,6 +23,17 @@ cudaError_t launch_cols_f64(int mode, int log2n, const ColArgs& a, cudaStream_t 
 cudaError_t launch_cols_blk_f32(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
 cudaError_t launch_cols_blk_f64(int mode, int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only);
 
+// Pair passes (two complex64 lines per thread, packed FP32; step_pair.cuh):
+// the persistent TMA inverse row passes (ROW_INV_NL, ROW_INV_NL_FWD) on the
+// blocked buffer, and the blocked column pass.  a.tma_grid / c.tma_grid hold
+// the SM count; cap_per_sm > 0 caps the CTAs per SM.  vshared: real
+// potential shared by the batch with an even number of fields.
+// cudaErrorNotSupported for a size without a pair kernel.
+cudaError_t launch_rows_pair(int mode, int log2n, const StepArgs& a, bool vshared, cudaStream_t s,
+                             bool prepare_only, int cap_per_sm);
+cudaError_t launch_cols_pair(int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only,
+                             int cap_per_sm);
+
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction
 int64_t noalloc_partials_max();     // capacity of the static partial-sum array

@@ -79,8 +79,9 @@ struct StepArgs {
   int nsteps;               // steps fused inside one launch (1-D full mode)
   uint32_t flags;
   int* status;              // plan status word (bounded waits record timeouts here)
-  int tma_grid;             // >0: TMA-fed persistent inverse row pass with this many CTAs
+  int tma_grid;             // >0: TMA-fed persistent inverse row pass on this many SMs
   const CUtensorMap* tmap;  // host pointer to the plan's tensor map of S (passed by value)
+  int cap_per_sm;           // >0: at most this many persistent CTAs per SM
 };
 
 struct ColArgs {
@@ -96,7 +97,8 @@ struct ColArgs {
   int comps;                // outer index % comps selects the propagator component
   int w;                    // columns per block (power of two)
   uint32_t flags;
-  int tma_grid;             // >0: persistent TMA-ring column pass with this many CTAs
+  int tma_grid;             // >0: persistent TMA-ring column pass on this many SMs
+  int cap_per_sm;           // >0: at most this many persistent CTAs per SM
 };
 
 template <typename T> struct NLP {

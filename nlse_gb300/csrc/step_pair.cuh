@@ -1,0 +1,401 @@
+// Split-step passes on pairs of complex64 lines (packed FP32, fft_pair.cuh).
+//
+// The same passes as step_kernels.cuh's persistent TMA kernels, with every
+// thread carrying one position of TWO lines:
+//   k_rows_pair_tma  two consecutive pixel-lines (two fields at the same row
+//                    when the batch has an even number of fields): inverse
+//                    row FFT, 1/N, nonlinear step, [next forward row FFT];
+//   k_cols_pair_tma  two adjacent columns of a blocked tile: forward column
+//                    FFT, propagator, inverse column FFT.
+// One-component fields, real or complex single-precision potential, real or
+// complex dz; the two-component, Rabi and pump terms stay on the scalar
+// kernels.  The nonlinear operator is the one of step_kernels.cuh
+// (kernels_gpu.py:4-65) evaluated on both lines at once; its reciprocal is
+// the hardware approximation refined by one Newton step (within an ulp of
+// the reference's division).
+#pragma once
+#include "fft_pair.cuh"
+#include "step_kernels.cuh"
+
+namespace nlse {
+
+// Per-line parameters of one nonlinear sub-step, lanes = (line a, line b).
+struct NLP2 {
+  float2 dz, nalpha, gs, ris, vs, dzi;
+  bool real_dz;
+};
+
+__device__ __forceinline__ NLP2 load_nlp2(const float* __restrict__ P, int64_t fa, int64_t fb,
+                                          int set) {
+  const float* pa = P + fa * kParamStride;
+  const float* pb = P + fb * kParamStride;
+  NLP2 r;
+  r.dz = f2(__ldg(pa + set * 16 + 0), __ldg(pb + set * 16 + 0));
+  r.nalpha = f2(-__ldg(pa + set * 16 + 1), -__ldg(pb + set * 16 + 1));
+  r.gs = f2(__ldg(pa + set * 16 + 2), __ldg(pb + set * 16 + 2));
+  r.ris = f2(1.0f / __ldg(pa + set * 16 + 4), 1.0f / __ldg(pb + set * 16 + 4));
+  r.vs = f2(__ldg(pa + set * 16 + 6), __ldg(pb + set * 16 + 6));
+  r.dzi = f2(__ldg(pa + 32 + set), __ldg(pb + 32 + set));
+  r.real_dz = r.dzi.x == 0.0f && r.dzi.y == 0.0f;
+  return r;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// exp(re) * (cos(im), sin(im)) for both lanes: the truncated series of
+// cis_exp (step_kernels.cuh) in packed form, the library functions for a
+// lane outside the series' range.
+__device__ __forceinline__ void pcis_exp(float2 re, float2 im, float2* cr, float2* ci) {
+  using R = CisRange<float>;
+  float2 e = f2s(float(inv_fact(R::EXP_DEG)));
+#pragma unroll
+  for (int k = R::EXP_DEG - 1; k >= 0; --k) e = fma2(e, re, f2s(float(inv_fact(k))));
+  const float2 x2 = mul2(im, im);
+  float2 s = f2s(float(sin_coef(R::SIN_K)));
+#pragma unroll
+  for (int k = R::SIN_K - 1; k >= 1; --k) s = fma2(s, x2, f2s(float(sin_coef(k))));
+  const float2 sn = fma2(mul2(im, x2), s, im);
+  float2 c = f2s(float(cos_coef(R::COS_K)));
+#pragma unroll
+  for (int k = R::COS_K - 1; k >= 0; --k) c = fma2(c, x2, f2s(float(cos_coef(k))));
+  *cr = mul2(e, c);
+  *ci = mul2(e, sn);
+  const bool ina = fabsf(re.x) <= R::RE && fabsf(im.x) <= R::IM;
+  const bool inb = fabsf(re.y) <= R::RE && fabsf(im.y) <= R::IM;
+  if (!(ina && inb)) {
+    if (!ina) cis_exp_lib(re.x, im.x, &cr->x, &ci->x);
+    if (!inb) cis_exp_lib(re.y, im.y, &cr->y, &ci->y);
+  }
+}
+
+// One nonlinear sub-step on one pair point; v = vscale * V of each lane
+// (v.x/v.y = real parts, vi = imaginary parts or zero).
+__device__ __forceinline__ cp2 nl_pair_point(cp2 x, const NLP2& p, bool has_v, float2 vre,
+                                             float2 vim) {
+  const float2 one = f2s(1.0f);
+  const float2 as = fma2(x.re, x.re, mul2(x.im, x.im));
+  const float2 den = fma2(as, p.ris, one);
+  float2 sat = f2(rcp_approx(den.x), rcp_approx(den.y));
+  sat = fma2(sat, fnma2(den, sat, one), sat);  // one Newton step
+  float2 im = mul2(mul2(p.gs, as), sat);
+  float2 re = mul2(p.nalpha, sat);
+  if (has_v) {
+    re = sub2(re, vim);
+    im = add2(im, vre);
+  }
+  float2 ar, ai;
+  if (p.real_dz) {
+    ar = mul2(re, p.dz);
+    ai = mul2(im, p.dz);
+  } else {
+    ar = fnma2(im, p.dzi, mul2(re, p.dz));
+    ai = fma2(re, p.dzi, mul2(im, p.dz));
+  }
+  float2 cr, ci;
+  pcis_exp(ar, ai, &cr, &ci);
+  return {fnma2(x.im, ci, mul2(x.re, cr)), fma2(x.re, ci, mul2(x.im, cr))};
+}
+
+// Shape of the pair row pass: PPC line pairs per CTA (at least 128 threads).
+template <int N>
+struct RowPair {
+  static constexpr int E = Shape<N>::E, TPL = N / E;
+  static constexpr int PPC = TPL >= 128 ? 1 : 128 / TPL;
+  static constexpr int LPC = 2 * PPC;
+  static constexpr int THREADS = PPC * TPL;
+  static constexpr int SLS = stage_len<float>(padded_len(N));
+};
+
+template <int N>
+__host__ __device__ constexpr size_t rows_pair_smem() {
+  return (size_t)2 * RowPair<N>::LPC * RowPair<N>::SLS * sizeof(float2) + kRowStages * sizeof(uint64_t);
+}
+
+// Persistent inverse row pass on pairs of lines of the blocked spectral
+// buffer (the k_rows_tma schedule: two line buffers alternate as TMA staging
+// and exchange buffers; every wait bounded).
+// VSHARED: the potential is real and both lines of every pair read the same
+// row of it (one potential for the batch and an even number of fields).
+template <int N, int MODE, bool VSHARED>
+__global__ void __launch_bounds__(RowPair<N>::THREADS) k_rows_pair_tma(
+    const StepArgs a, const __grid_constant__ CUtensorMap tmS) {
+  using RP = RowPair<N>;
+  using C = float2;
+  constexpr int E = RP::E, TPL = RP::TPL, W = BlkW<float>::W, NB = N / W, LPC = RP::LPC,
+                SLS = RP::SLS;
+  constexpr int BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
+  constexpr unsigned ROW_BYTES = N * sizeof(C);
+  static_assert((SLS * sizeof(C)) % 128 == 0 && (BOXB * W * sizeof(C)) % 128 == 0,
+                "tensor-map copies need 128-byte aligned shared destinations");
+  static_assert(padded_len(N) * sizeof(float4) <= 2 * SLS * sizeof(C),
+                "a pair's exchange fits in its two staging lines");
+  constexpr int NEX = fft_exchanges(N, E);
+  static_assert(NEX == 1 || NEX == 2, "one or two exchanges per transform");
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* X = reinterpret_cast<C*>(smraw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * SLS);
+  auto buf = [&](int b, int l) { return X + (b * LPC + l) * SLS; };
+  const int pp = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  const unsigned nq = (unsigned)a.nq;
+  const unsigned ngroups = (nq + LPC - 1) / LPC;
+  const unsigned nf = nq / (unsigned)a.lines_per_comp;
+  auto q_f = [&](unsigned q) { return q % nf; };
+  auto q_y = [&](unsigned q) { return q / nf; };
+  auto issue = [&](int b, unsigned g) {
+    const unsigned q0 = g * LPC;
+    const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+    mbar_arrive_expect_tx(&bar[b], nl * ROW_BYTES);
+    for (unsigned l = 0; l < nl; ++l) {
+      const unsigned f = q_f(q0 + l), y = q_y(q0 + l);
+#pragma unroll
+      for (int bx = 0; bx < NBOX; ++bx)
+        tensor_load_4d(buf(b, (int)l) + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB, (int)f, &bar[b]);
+    }
+  };
+  auto prefetch = [&](int b, unsigned gn) {
+    if (gn < ngroups) {
+      fence_proxy_async_smem();
+      issue(b, gn);
+    }
+  };
+  const float2* tw = reinterpret_cast<const float2*>(a.tw);
+  const float* P = a.params_f32;
+  const bool has_v = a.flags & F_HAS_V;
+  const bool v_cplx = a.flags & F_V_COMPLEX;
+  const float2 sc = f2s(a.inv_nf);
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kRowStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x < ngroups) issue(0, blockIdx.x);
+  int it = 0;
+  for (unsigned g = blockIdx.x; g < ngroups; g += gridDim.x, ++it) {
+    const int st = it & 1;
+    const unsigned par = (it >> 1) & 1;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+      }
+      return;
+    }
+    // pairs past the end (last group) compute on in-range lines and store nothing
+    const unsigned qa = g * LPC + 2 * pp;
+    const bool act = qa + 1 < nq;
+    const unsigned qca = act ? qa : nq - 2, qcb = qca + 1;
+    const int64_t fa = q_f(qca), ma = q_y(qca), fb = q_f(qcb), mb = q_y(qcb);
+    cp2 x[E];
+    {
+      const C* la = buf(st, 2 * pp);
+      const C* lb = buf(st, 2 * pp + 1);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const C u = la[t + j * TPL], v = lb[t + j * TPL];
+        x[j] = {f2(u.x, v.x), f2(u.y, v.y)};
+      }
+    }
+    // potential: VSHARED (both lines read the same row of one shared real
+    // potential) prefetches one value per position before the transform;
+    // otherwise each lane's value is read when the nonlinear step needs it
+    const int64_t va = fa * a.v_fstride + ma * (int64_t)N + t;
+    const int64_t vb = fb * a.v_fstride + mb * (int64_t)N + t;
+    float vpre[VSHARED ? E : 1];
+    if constexpr (VSHARED) {
+      if (has_v) {
+        const float* V1 = reinterpret_cast<const float*>(a.V);
+#pragma unroll
+        for (int j = 0; j < E; ++j) vpre[j] = __ldg(V1 + va + j * TPL);
+      }
+    }
+    __syncthreads();  // every thread has read its lines from buffer st
+    float4* sA = reinterpret_cast<float4*>(buf(st, 2 * pp));
+    float4* sB = reinterpret_cast<float4*>(buf(st ^ 1, 2 * pp));
+    pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = {mul2(x[j].re, sc), mul2(x[j].im, sc)};
+    // V' = vscale * V rounded in single precision, as the reference's k/2*V array
+    auto nl_all = [&](int set) {
+      const NLP2 p = load_nlp2(P, fa, fb, set);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        if (!has_v) {
+          x[j] = nl_pair_point(x[j], p, false, f2s(0.f), f2s(0.f));
+        } else if constexpr (VSHARED) {
+          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2s(vpre[j])), f2s(0.f));
+        } else if (v_cplx) {
+          const float2* V2 = reinterpret_cast<const float2*>(a.V);
+          const float2 u = __ldg(V2 + va + j * TPL), w = __ldg(V2 + vb + j * TPL);
+          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2(u.x, w.x)), mul2(p.vs, f2(u.y, w.y)));
+        } else {
+          const float* V1 = reinterpret_cast<const float*>(a.V);
+          const float2 u = f2(__ldg(V1 + va + j * TPL), __ldg(V1 + vb + j * TPL));
+          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, u), f2s(0.f));
+        }
+      }
+    };
+    if (!(a.flags & F_NO_POST)) nl_all(0);
+    if constexpr (MODE == ROW_INV_NL_FWD) {
+      if (a.flags & F_PRE_NL) nl_all(1);
+      pfft_hook<N, E, false, true, NEX == 1>(x, t, sA, 1, tw, [&] {
+        if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
+      });
+      if (act) {
+        const int64_t lpc = a.lines_per_comp, dstr = (int64_t)TPL * lpc;
+        C* da = reinterpret_cast<C*>(a.S) + fa * a.pix + ((t / W) * lpc + ma) * W + (t % W);
+        C* db = reinterpret_cast<C*>(a.S) + fb * a.pix + ((t / W) * lpc + mb) * W + (t % W);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          da[j * dstr] = f2(x[j].re.x, x[j].im.x);
+          db[j * dstr] = f2(x[j].re.y, x[j].im.y);
+        }
+      }
+    } else {
+      __syncthreads();  // B is no longer read
+      if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
+      if (act) {
+        C* da = reinterpret_cast<C*>(a.A) + fa * a.pix + ma * N + t;
+        C* db = reinterpret_cast<C*>(a.A) + fb * a.pix + mb * N + t;
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          da[j * TPL] = f2(x[j].re.x, x[j].im.x);
+          db[j * TPL] = f2(x[j].re.y, x[j].im.y);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace nlse
+
+namespace nlse {
+
+// Persistent column pass over the blocked spectral buffer on column pairs:
+// one tile (W = 4 columns x N rows, one contiguous run) per iteration by
+// bulk copy into a two-stage ring, as k_cols_blk_tma; thread (t, p) carries
+// columns 2p, 2p+1 at rows t + j*TPL (p alternates fastest, so a quarter-warp
+// reads 128 contiguous bytes of the tile).  The exchanges use the staging
+// tile just read (A) and one exchange tile (B), the pairs interleaved
+// (element i of pair p at padi(i) * 2 + p, float4).  Forward column FFT,
+// propagator, inverse column FFT; the propagator (blocked, complex64) values
+// of the tile are requested before the forward transform.
+template <int N>
+__host__ __device__ constexpr size_t cols_pair_smem() {
+  return cols_tma_smem<float, N>();
+}
+
+template <int N>
+__global__ void __launch_bounds__(2 * (N / Shape<N>::E), 1) k_cols_pair_tma(const ColArgs a) {
+  using C = float2;
+  constexpr int E = Shape<N>::E, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
+  constexpr int SLW = stage_len<float>(padded_len(N) * W);
+  static_assert((SLW * sizeof(C)) % 128 == 0, "bulk copies need aligned shared destinations");
+  static_assert(padded_len(N) * 2 * sizeof(float4) <= SLW * sizeof(C),
+                "both pairs' exchanges fit in one staging tile");
+  constexpr unsigned TILE_BYTES = TILE * sizeof(C);
+  constexpr int NEX = fft_exchanges(N, E);
+  constexpr bool DB = NEX > 0 && NEX % 2 == 0;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* stage = reinterpret_cast<C*>(smraw);
+  C* xch = stage + kColStages * SLW;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + SLW);
+  constexpr bool TWS = cols_tma_tws<float, N>();
+  C* twc = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(bar) + 16);
+  if constexpr (TWS) load_tw_compact<float, N, E>(twc, reinterpret_cast<const C*>(a.tw));
+  const C* tw = TWS ? twc : reinterpret_cast<const C*>(a.tw);
+  C* S = reinterpret_cast<C*>(a.A);
+  const int p = threadIdx.x & 1, t = threadIdx.x >> 1;
+  const int64_t ntiles = a.nblocks;
+  const int64_t nouter = ntiles / a.ncb;
+  auto tile_o = [&](int64_t i) { return i % nouter; };
+  auto tile_b = [&](int64_t i) { return i / nouter; };
+  auto tile_ptr = [&](int64_t i) { return S + tile_o(i) * a.outer_stride + tile_b(i) * TILE; };
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kColStages; ++st) {
+      const int64_t i = blockIdx.x + (int64_t)st * gridDim.x;
+      if (i < ntiles) {
+        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+        bulk_load(stage + st * SLW, tile_ptr(i), TILE_BYTES, &bar[st]);
+      }
+    }
+  }
+  auto refill = [&](int st, int64_t i) {
+    const int64_t inext = i + (int64_t)kColStages * gridDim.x;
+    if (inext < ntiles) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+      bulk_load(stage + st * SLW, tile_ptr(inext), TILE_BYTES, &bar[st]);
+    }
+  };
+  int it = 0;
+  for (int64_t i = blockIdx.x; i < ntiles; i += gridDim.x, ++it) {
+    const int st = it % kColStages;
+    const unsigned par = (it / kColStages) & 1;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+        if (i + gridDim.x < ntiles)
+          mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kColStages) & 1);
+      }
+      return;
+    }
+    cp2 x[E];
+    {
+      const float4* sp = reinterpret_cast<const float4*>(stage + st * SLW) + t * 2 + p;
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const float4 v = sp[j * TPL * 2];
+        x[j] = {f2(v.x, v.z), f2(v.y, v.w)};
+      }
+    }
+    const int64_t o = tile_o(i);
+    const int64_t toff = tile_b(i) * (int64_t)TILE + (int64_t)t * W + 2 * p;
+    const int64_t pb = (o % a.comps) * a.prop_cstride + toff;
+    // propagator values of both columns (L2-resident), used after the forward FFT
+    float4 pre[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      pre[j] = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const C*>(a.prop) + pb +
+                                                     (int64_t)j * TPL * W));
+    __syncthreads();  // every thread has read stage st
+    float4* sA = reinterpret_cast<float4*>(stage + st * SLW) + p;
+    float4* sB = reinterpret_cast<float4*>(xch) + p;
+    if constexpr (DB) {
+      pfft_db<N, E, 1, false, 0, 1, TWS>(x, t, sA, sB, 2, tw);
+    } else {
+      if (threadIdx.x == 0) refill(st, i);
+      pfft_rest<N, E, 1, false, false, TWS>(x, t, sB, 2, tw);
+    }
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float2 pr = f2(pre[j].x, pre[j].z), pi = f2(pre[j].y, pre[j].w);
+      x[j] = {fnma2(x[j].im, pi, mul2(x[j].re, pr)), fma2(x[j].re, pi, mul2(x[j].im, pr))};
+    }
+    if constexpr (DB) {
+      pfft_db<N, E, 1, true, 0, 1, TWS>(x, t, sA, sB, 2, tw);
+      if (threadIdx.x == 0) refill(st, i);
+    } else {
+      pfft_rest<N, E, 1, true, false, TWS>(x, t, sB, 2, tw);
+    }
+    float4* g = reinterpret_cast<float4*>(S + o * a.outer_stride + toff);
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      g[(int64_t)j * TPL * 2] = make_float4(x[j].re.x, x[j].im.x, x[j].re.y, x[j].im.y);
+  }
+}
+
+}  // namespace nlse

@@ -10,7 +10,6 @@ from __future__ import annotations
 import ctypes as ct
 import itertools
 import math
-import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -94,6 +93,22 @@ class Plan:
         """Choose the 2-D passes' kernel variants (nlse_plan_set_kernels)."""
         _lib.check(self.lib.nlse_plan_set_kernels(self.handle, int(rows_tma), int(cols_tma)),
                    "kernel variant")
+
+    def set_variant(self, rows: int, cols: int, rows_cap: int = 0, cols_cap: int = 0) -> None:
+        """Choose the 2-D passes' variants and CTAs per SM (nlse_plan_set_variant)."""
+        _lib.check(self.lib.nlse_plan_set_variant(self.handle, int(rows), int(cols), int(rows_cap),
+                                                  int(cols_cap)), "kernel variant")
+
+    def get_variant(self) -> dict:
+        """Current variant codes, CTA caps and the available variants (code lists)."""
+        v = [ct.c_int32() for _ in range(4)]
+        m = [ct.c_uint32() for _ in range(2)]
+        _lib.check(self.lib.nlse_plan_get_variant(self.handle, *[ct.byref(x) for x in v],
+                                                  *[ct.byref(x) for x in m]), "kernel variant")
+        return {"rows": v[0].value, "cols": v[1].value, "rows_cap": v[2].value,
+                "cols_cap": v[3].value,
+                "rows_avail": [i for i in range(3) if m[0].value >> i & 1],
+                "cols_avail": [i for i in range(3) if m[1].value >> i & 1]}
 
     def get_kernels(self) -> tuple:
         """(rows_tma, cols_tma, rows_tma available, cols_tma available)."""
@@ -336,39 +351,32 @@ def nonlocal_spectrum(profile, grid: tuple, dtype: torch.dtype, device) -> tuple
     return pads, khat.contiguous()
 
 
-_STAGE: dict = {}
-_STAGE_LOCK = threading.Lock()
-STAGE_MIN_BYTES = 8 << 20
+PINNED_MIN_BYTES = 8 << 20
 
 
 def to_host(t: torch.Tensor) -> torch.Tensor:
-    """A new host tensor with the values of t.  Large device tensors go
-    through a pinned staging buffer kept per device (the device copy at the
-    pinned rate, then torch's multi-threaded host copy): a direct copy into
-    new pageable memory runs at about a tenth of that.  release_staging()
-    returns the buffers."""
-    if not t.is_cuda or t.numel() * t.element_size() < STAGE_MIN_BYTES:
+    """A new host tensor with the values of t.
+
+    Large results land in page-locked memory from torch's caching host
+    allocator: the device copy then runs at the host link's rate and no
+    second host copy is needed (a copy into newly mapped pageable memory runs
+    at a tenth of that, its page faults included).  A freed result's block
+    is reused by the next result of the same size; release_staging() returns
+    the cached blocks to the system."""
+    if not t.is_cuda or t.numel() * t.element_size() < PINNED_MIN_BYTES:
         return t.cpu()
     t = t.contiguous()
-    nbytes = t.numel() * t.element_size()
-    with _STAGE_LOCK:
-        key = t.device.index
-        buf = _STAGE.get(key)
-        if buf is None or buf.numel() < nbytes:
-            _STAGE.pop(key, None)
-            buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
-            _STAGE[key] = buf
-        view = buf[:nbytes].view(t.dtype).view(t.shape)
-        view.copy_(t)  # waits for the producing stream
-        out = torch.empty(t.shape, dtype=t.dtype)
-        out.copy_(view)
+    out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    out.copy_(t)  # waits for the producing stream, then copies at the pinned rate
     return out
 
 
 def release_staging() -> None:
-    """Free the pinned staging buffers of to_host."""
-    with _STAGE_LOCK:
-        _STAGE.clear()
+    """Return the page-locked blocks cached for host results to the system
+    (blocks still held by live results are kept)."""
+    empty = getattr(torch._C, "_host_emptyCache", None)
+    if empty is not None:
+        empty()
 
 
 def to_device(x, device, dtype=None) -> torch.Tensor:

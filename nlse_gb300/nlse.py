@@ -236,7 +236,9 @@ class NLSE:
         dev = self._device
         src = engine.to_device(E_in, dev)
         A = torch.empty_like(src)
-        A_sq = torch.zeros(A.shape, dtype=A.real.dtype, device=dev)
+        # split_step's |A|^2 argument: the fused kernels form |A|^2 in registers and
+        # never read it, so it is not zero-filled
+        A_sq = torch.empty(A.shape, dtype=A.real.dtype, device=dev)
         if normalize:
             lead = self._lead_shape(tuple(A.shape))
             nseg = int(np.prod(lead)) * self._comps if lead else self._comps

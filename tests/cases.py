@@ -101,3 +101,67 @@ def mixed_batch(groups, seed=0, dtype=np.complex64, cls=None, dz=5e-5):
         E = np.exp(-(sim.XX[None] ** 2 + sim.YY[None] ** 2) / waist[:, None, None] ** 2)
         jobs.append((sim, E.astype(dtype)))
     return jobs
+
+
+# ---------------------------------------------------------------------------
+# the benchmark configurations at their stated sizes (fixtures under
+# tests/golden/fullsize/, made by tests/golden/make_parity.py with the
+# reference's own classes; the same builders serve the product's tests)
+# ---------------------------------------------------------------------------
+def nlse2048_inputs(cls, dtype, N=2048, seed=0):
+    """The 2048^2 configuration: Gaussian beam times (1 + 0.01 (a + ib)), a, b
+    standard normal from default_rng(seed), potential well, dz = 2e-5 m."""
+    sim = cls(ALPHA, POWER, WINDOW, N2, None, L, NX=N, NY=N, Isat=ISAT)
+    sim.delta_z = 2e-5
+    rng = np.random.default_rng(seed)
+    E = gaussian(sim.XX, sim.YY)
+    E = E * (1 + 0.01 * (rng.standard_normal(E.shape) + 1j * rng.standard_normal(E.shape)))
+    sim.V = potential(sim.XX, sim.YY).astype(np.complex64)
+    return sim, E.astype(dtype)
+
+
+def cnlse1024_inputs(cls, dtype, N=1024):
+    """The coupled 1024^2 configuration: waists 1.5 / 0.5 mm, powers 0.5 / 0.05 W,
+    n2 = n22 = -1.6e-9, n12 = -0.8e-9, Gaussian nonlocal kernel (sigma 100 um on a
+    67^2 support, normalised, set through nl_profile), L = 20 mm, dz = 5e-5."""
+    sim = cls(ALPHA, 0.5, WINDOW, N2, -0.8e-9, None, 20e-3, NX=N, NY=N, Isat=ISAT,
+              nl_length=100e-6)
+    sim.delta_z = 5e-5
+    sim.power2 = 0.05
+    sim.n22 = N2
+    r = np.arange(-33, 34) * sim.delta_X
+    kern = np.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * (100e-6) ** 2))
+    sim.nl_profile = kern / kern.sum()
+    E = np.array([gaussian(sim.XX, sim.YY, w) for w in (1.5e-3, 0.5e-3)])
+    return sim, E.astype(dtype)
+
+
+MIXED_GROUPS = [(96, 256), (48, 512), (16, 1024), (4, 2048)]
+MIXED_SEED = 11
+
+
+def mixed_field0(cls, dtype, group: int):
+    """Field 0 of group `group` of the 164-field batch (mixed_batch, seed 11) as a
+    one-field simulation with its per-field arrays: power (1,), n2 (1, 1, 1)
+    float64, V (1, N, N)."""
+    jobs = mixed_batch(MIXED_GROUPS, seed=MIXED_SEED, dtype=dtype, cls=cls)
+    sim_b, E_b = jobs[group]
+    N = E_b.shape[-1]
+    sim = cls(ALPHA, np.asarray(sim_b.power)[:1], WINDOW, np.asarray(sim_b.n2)[:1], None, L,
+              NX=N, NY=N, Isat=ISAT)
+    sim.delta_z = sim_b.delta_z
+    sim.V = np.asarray(sim_b.V)[:1].copy()
+    return sim, E_b[:1].copy()
+
+
+SAMPLES = 128  # full-size outputs are compared on a SAMPLES x SAMPLES grid
+
+
+def subsample(E):
+    s = E.shape[-1] // SAMPLES
+    return np.ascontiguousarray(np.asarray(E)[..., ::s, ::s])
+
+
+def power_fp64(E):
+    e = np.asarray(E).astype(np.complex128)
+    return (e.real ** 2 + e.imag ** 2).sum(axis=(-2, -1))

@@ -40,7 +40,10 @@ def _engine(sim, A, V):
     return plan, op
 
 
-def test_batch_fields_equal_their_single_field_runs():
+def test_batch_fields_equal_their_single_field_runs(monkeypatch):
+    # one kernel variant for both plans: the autotuner may pick different ones for
+    # 8 fields and for 1, and variants agree only to rounding
+    monkeypatch.setenv("NLSE_AUTOTUNE", "0")
     sim, E, V = _setup(B)
     z = 19.5 * DZ
     out = sim.out_field(torch.from_numpy(E).cuda(), z, verbose=False)

@@ -33,6 +33,21 @@ def test_product_matches_reference_fixture(name):
         assert r["ok"], r
 
 
+@pytest.mark.parametrize("name", gc.SHORT)
+def test_product_matches_reference_at_20_steps(name):
+    """complex64 against the reference's own complex64 result after 20 steps:
+    rel-L2 <= 1e-5 (the reference's FFT spread there is ~1e-6)."""
+    f = gc.load_short(name)
+    got = gc.run(name, "product", steps=int(f["steps"]))
+    ref = f["out"]
+    assert got.shape == ref.shape and got.dtype == ref.dtype
+    err = rel_l2(got, ref)
+    spr = max(rel_l2(f["out_numpy"], ref), rel_l2(f["out_torch"], ref))
+    print(f"{name} ({int(f['steps'])} steps): product vs reference {err:.2e}, "
+          f"reference FFT spread {spr:.2e}")
+    assert err <= 1e-5, err
+
+
 @pytest.mark.parametrize("tag", ["c64", "c128"])
 def test_elementwise_kernels_match_reference(tag):
     """nlse_nonlinear against kernels_gpu.nl_prop / nl_prop_c / rabi_coupling outputs."""

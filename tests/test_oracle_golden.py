@@ -62,3 +62,28 @@ def test_benchmark_step_counts():
     assert orc.count_steps(10e-3, 5e-5) == 201
     assert orc.count_steps(10e-3, 2e-5) == 501
     assert orc.count_steps(20e-3, 5e-5) == 400
+
+
+@pytest.mark.parametrize("name", gc.SHORT)
+def test_oracle_matches_reference_at_20_steps(name):
+    f = gc.load_short(name)
+    got = gc.run(name, "oracle", steps=int(f["steps"]))
+    assert got.shape == f["out"].shape and got.dtype == f["out"].dtype
+    assert rel_l2(got, f["out"]) <= 1e-7
+
+
+def test_reference_complex64_fft_spread():
+    """The reference's own complex64 results, recomputed with the NumPy and the
+    torch (oneMKL) FFT behind its VkFFT stand-in instead of scipy's: they agree
+    to ~1e-6 after 20 steps, and drift past 1e-5 at the cases' full lengths
+    (200 to 640 steps), which is why the full-length complex64 gate is the
+    reference's own spread, not 1e-5."""
+    short = {n: max(rel_l2(f["out_numpy"], f["out"]), rel_l2(f["out_torch"], f["out"]))
+             for n in gc.SHORT for f in [gc.load_short(n)]}
+    assert max(short.values()) < 3e-6, short
+    full = {n: gc.spread(n) for n in gc.FIXTURES if "c64" in n}
+    assert max(full.values()) > 1e-5, full
+    over = sorted(n for n, v in full.items() if v > 1e-5)
+    assert {"nlse2d_c64_single", "nlse2d_c64_noise_noV", "cnlse_c64_single_rabi"} <= set(over)
+    # complex128: the backends agree to 1e-12 at full length
+    assert all(gc.spread(n) < 1e-12 for n in gc.FIXTURES if "c128" in n and "cpu" not in n)
