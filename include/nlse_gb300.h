@@ -96,6 +96,16 @@ typedef struct {
   const void* nl_khat;   /* nonlocal response: spectrum (field dtype) of the kernel placed on the
                             plan's padded grid with its centre at the origin, or NULL for a local
                             response; see nlse_plan_set_nonlocal */
+  const void* nl_maps;   /* spatially varying nonlinear coefficients of a one-component field
+                            (the reference's n2, alpha or Isat given as arrays over the grid,
+                            NLSE/nlse.py:309-328 and kernels_gpu.py:4-65), or NULL: planes
+                            [3][map fields][pixels] in the field's real type (float for
+                            complex64, double for complex128) holding g = k/2 n2 c eps0,
+                            alpha/2 and 1/Isat' (Isat' = 2 Isat/(eps0 c)); a plane whose bit is
+                            set in maps_mask replaces the parameter block's per-field value */
+  int64_t maps_fstride;  /* elements between two fields' maps in a plane; 0 = shared */
+  int64_t maps_plane;    /* elements between two planes */
+  int32_t maps_mask;     /* bit 0: g plane, bit 1: alpha/2 plane, bit 2: 1/Isat' plane */
 } nlse_operator;
 
 /* ABI version of the loaded library (NLSE_ABI_VERSION). */
@@ -183,9 +193,11 @@ int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
 #define NLSE_ROWS_LINE 0
 #define NLSE_ROWS_TMA 1
 #define NLSE_ROWS_PAIR 2
+#define NLSE_ROWS_PAIR8 3 /* NLSE_ROWS_PAIR with 8 positions per thread: twice the threads */
 #define NLSE_COLS_TILE 0
 #define NLSE_COLS_TMA 1
 #define NLSE_COLS_PAIR 2
+#define NLSE_COLS_PAIR8 3 /* NLSE_COLS_PAIR with 8 positions per thread: twice the threads */
 int nlse_plan_set_variant(nlse_plan plan, int32_t rows, int32_t cols, int32_t rows_ctas_per_sm,
                           int32_t cols_ctas_per_sm);
 int nlse_plan_get_variant(nlse_plan plan, int32_t* rows, int32_t* cols, int32_t* rows_ctas_per_sm,

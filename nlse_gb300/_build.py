@@ -31,8 +31,10 @@ SOURCES = [
     "rows_f64_c2.cu",
     "cols_f32.cu",
     "cols_f64.cu",
-    "rows_pair_mid.cu",
-    "rows_pair_last.cu",
+    "rows_pair16_mid.cu",
+    "rows_pair16_last.cu",
+    "rows_pair8_mid.cu",
+    "rows_pair8_last.cu",
     "cols_pair.cu",
     "fno.cu",
 ]

@@ -181,7 +181,8 @@ namespace {
 // The pair row pass serves this launch: complex64 one-component field on
 // the blocked buffer through the tensor map, no Rabi, pump or external |A|^2.
 bool rows_pair_fits(const nlse_plan_s* p, int mode, const StepArgs& a) {
-  return p->rows_var == NLSE_ROWS_PAIR && p->d.dtype == NLSE_C64 && a.comps == 1 &&
+  return (p->rows_var == NLSE_ROWS_PAIR || p->rows_var == NLSE_ROWS_PAIR8) &&
+         p->d.dtype == NLSE_C64 && a.comps == 1 &&
          (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (a.flags & F_IN_BLK) && a.tmap &&
          a.tma_grid > 0 && !(a.flags & (F_RABI | F_PUMP | F_PROBE | F_ASQ_EXT)) &&
          (!(a.flags & F_HAS_V) || (a.flags & F_V_F32)) && a.nq % 2 == 0 &&
@@ -192,15 +193,18 @@ cudaError_t rows(const nlse_plan_s* p, int mode, int log2n, const StepArgs& a, c
                  bool prep = false) {
   if (prep && p->d.dtype == NLSE_C64 && a.comps == 1 &&
       (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (p->rows_avail >> NLSE_ROWS_PAIR & 1)) {
-    const cudaError_t e = launch_rows_pair(mode, log2n, a, false, s, true, 0);
-    if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+    for (int ep : {16, 8}) {
+      const cudaError_t e = launch_rows_pair(mode, log2n, a, false, s, true, 0, ep);
+      if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+    }
   }
   if (!prep && rows_pair_fits(p, mode, a)) {
     // the potential row is shared by both lines of every pair when one real
     // potential serves an even number of fields (lines are field-fastest)
     const bool vshared = (a.flags & F_HAS_V) && !(a.flags & F_V_COMPLEX) && a.v_fstride == 0 &&
                          p->d.nfields % 2 == 0;
-    const cudaError_t e = launch_rows_pair(mode, log2n, a, vshared, s, false, p->rows_cap);
+    const int ep = p->rows_var == NLSE_ROWS_PAIR8 ? 8 : 16;
+    const cudaError_t e = launch_rows_pair(mode, log2n, a, vshared, s, false, p->rows_cap, ep);
     if (e != cudaErrorNotSupported) return e;
   }
   if (p->d.dtype == NLSE_C64)
@@ -220,11 +224,15 @@ cudaError_t cols_blk(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a
                      bool prep = false) {
   if (p->d.dtype == NLSE_C64 && mode == COL_FWD_PROP_INV) {
     if (prep && (p->cols_avail >> NLSE_COLS_PAIR & 1)) {
-      const cudaError_t e = launch_cols_pair(log2n, a, s, true, 0);
-      if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+      for (int ep : {16, 8}) {
+        const cudaError_t e = launch_cols_pair(log2n, a, s, true, 0, ep);
+        if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
+      }
     }
-    if (!prep && p->cols_var == NLSE_COLS_PAIR && a.tma_grid > 0 && !(a.flags & F_PROP_C128)) {
-      const cudaError_t e = launch_cols_pair(log2n, a, s, false, p->cols_cap);
+    if (!prep && (p->cols_var == NLSE_COLS_PAIR || p->cols_var == NLSE_COLS_PAIR8) &&
+        a.tma_grid > 0 && !(a.flags & F_PROP_C128)) {
+      const int ep = p->cols_var == NLSE_COLS_PAIR8 ? 8 : 16;
+      const cudaError_t e = launch_cols_pair(log2n, a, s, false, p->cols_cap, ep);
       if (e != cudaErrorNotSupported) return e;
     }
   }
@@ -353,6 +361,13 @@ StepArgs row_args(const nlse_plan_s* p, void* A, const nlse_operator* op) {
     if (op->rabi && d.comps == 2 && op->scheme == 0) f |= F_RABI;
     if (op->pump_r && d.comps == 2) f |= F_PUMP;
     if (op->probe_r && d.comps == 2) f |= F_PROBE;
+    if (op->nl_maps && op->maps_mask) {
+      f |= F_MAPS;
+      a.maps = op->nl_maps;
+      a.maps_fstride = op->maps_fstride;
+      a.maps_plane = op->maps_plane;
+      a.maps_mask = op->maps_mask;
+    }
     a.flags = f;
   }
   return a;
@@ -369,6 +384,14 @@ int check_op(const nlse_plan_s* p, const nlse_operator* op) {
     return fail(NLSE_ERR_ARG, "pump/probe spatial profile given without time profile");
   if ((op->pump_r || op->probe_r) && (p->d.comps != 2 || p->d.ndim != 2))
     return fail(NLSE_ERR_UNSUPPORTED, "pump/probe terms need a two-component 2-D field");
+  if (op->nl_maps && op->maps_mask) {
+    if (p->d.comps != 1)
+      return fail(NLSE_ERR_UNSUPPORTED, "coefficient maps are for one-component fields");
+    if ((op->maps_mask & ~7) || op->maps_fstride < 0 || op->maps_plane < p->pix ||
+        (op->maps_fstride && op->maps_plane < op->maps_fstride * p->d.nfields))
+      return fail(NLSE_ERR_ARG, "coefficient maps: mask bits 0..2, plane of at least the "
+                  "maps' elements");
+  }
   return NLSE_OK;
 }
 
@@ -692,10 +715,10 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     const bool pair = !(penv && penv[0] == '0') && d.dtype == NLSE_C64 && d.comps == 1;
     if (p->rows_tma_ok) p->rows_avail |= 1u << NLSE_ROWS_TMA;
     if (p->rows_tma_ok && pair && p->lg[1] >= 6 && p->lg[1] <= 12)
-      p->rows_avail |= 1u << NLSE_ROWS_PAIR;
+      p->rows_avail |= (1u << NLSE_ROWS_PAIR) | (1u << NLSE_ROWS_PAIR8);
     if (p->cols_tma_ok) p->cols_avail |= 1u << NLSE_COLS_TMA;
     if (p->cols_tma_ok && pair && p->lg[0] >= 6 && p->lg[0] <= 11)
-      p->cols_avail |= 1u << NLSE_COLS_PAIR;
+      p->cols_avail |= (1u << NLSE_COLS_PAIR) | (1u << NLSE_COLS_PAIR8);
     p->rows_var = (p->rows_avail >> NLSE_ROWS_PAIR & 1) ? NLSE_ROWS_PAIR
                   : p->rows_tma                          ? NLSE_ROWS_TMA
                                                          : NLSE_ROWS_LINE;
@@ -920,9 +943,9 @@ int nlse_plan_set_variant(nlse_plan p, int32_t rows, int32_t cols, int32_t rows_
                           int32_t cols_ctas_per_sm) {
   g_err.clear();
   if (!p) return fail(NLSE_ERR_ARG, "null plan");
-  if (rows < 0 || rows > 2 || cols < 0 || cols > 2 || rows_ctas_per_sm < 0 ||
+  if (rows < 0 || rows > 3 || cols < 0 || cols > 3 || rows_ctas_per_sm < 0 ||
       cols_ctas_per_sm < 0 || rows_ctas_per_sm > 32 || cols_ctas_per_sm > 32)
-    return fail(NLSE_ERR_ARG, "variant codes 0..2, CTAs per SM 0..32");
+    return fail(NLSE_ERR_ARG, "variant codes 0..3, CTAs per SM 0..32");
   if (!(p->rows_avail >> rows & 1))
     return fail(NLSE_ERR_UNSUPPORTED, "row pass variant %d is not available for this plan", rows);
   if (!(p->cols_avail >> cols & 1))

@@ -29,10 +29,11 @@ cudaError_t launch_cols_blk_f64(int mode, int log2n, const ColArgs& a, cudaStrea
 // the SM count; cap_per_sm > 0 caps the CTAs per SM.  vshared: real
 // potential shared by the batch with an even number of fields.
 // cudaErrorNotSupported for a size without a pair kernel.
+// ep: positions per thread and line, 16 or 8 (twice the threads per line).
 cudaError_t launch_rows_pair(int mode, int log2n, const StepArgs& a, bool vshared, cudaStream_t s,
-                             bool prepare_only, int cap_per_sm);
+                             bool prepare_only, int cap_per_sm, int ep);
 cudaError_t launch_cols_pair(int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only,
-                             int cap_per_sm);
+                             int cap_per_sm, int ep);
 
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction

@@ -112,6 +112,7 @@ __global__ void k_nl_point(const StepArgs a) {
     const int64_t vi = f * a.v_fstride + px;
     const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
     if constexpr (NC == 1) {
+      if (a.flags & F_MAPS) apply_maps<T>(p0, a, f, px);
       A[i0] = nl_point<T, false>(x0, a0, T(0), p0, has_v, v0);
     } else {
       const int64_t i1 = i0 + a.pix;
@@ -206,6 +207,7 @@ __global__ void k_nl_point_pad(const StepArgs a, const cpx<T>* __restrict__ X, i
     const int64_t vi = f * a.v_fstride + pxl;
     const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
     if constexpr (NC == 1) {
+      if (a.flags & F_MAPS) apply_maps<T>(p0, a, f, pxl);
       A[i0] = nl_point<T, false>(A[i0], c.x, T(0), p0, has_v, v0);
     } else {
       const int64_t i1 = i0 + a.pix;

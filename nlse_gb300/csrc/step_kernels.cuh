@@ -44,6 +44,7 @@ enum : uint32_t {
                           // for a complex64 V with a complex128 field
   F_IN_BLK = 1u << 10,    // row pass reads the blocked spectral buffer S
   F_OUT_BLK = 1u << 11,   // row pass writes the blocked spectral buffer S
+  F_MAPS = 1u << 12,      // per-pixel g / alpha / 1/Isat planes (one-component fields)
 };
 
 // Blocked spectral layout of a 2-D slab [NY][NX]: element (y, x) at
@@ -82,7 +83,21 @@ struct StepArgs {
   int tma_grid;             // >0: TMA-fed persistent inverse row pass on this many SMs
   const CUtensorMap* tmap;  // host pointer to the plan's tensor map of S (passed by value)
   int cap_per_sm;           // >0: at most this many persistent CTAs per SM
+  const void* maps;         // T planes [3][map fields][pix]: g, alpha/2, 1/Isat' (F_MAPS)
+  int64_t maps_fstride;     // field stride of the planes (0: shared)
+  int64_t maps_plane;       // elements between planes
+  int maps_mask;            // planes present (bit 0 g, 1 alpha, 2 1/Isat')
 };
+
+// Per-pixel nonlinear coefficients: the planes present replace the line's
+// per-field values (idx = pixel index within the field).
+template <typename T, typename P>
+__device__ __forceinline__ void apply_maps(P& p, const StepArgs& a, int64_t f, int64_t idx) {
+  const T* M = reinterpret_cast<const T*>(a.maps) + f * a.maps_fstride + idx;
+  if (a.maps_mask & 1) p.gs = __ldg(M);
+  if (a.maps_mask & 2) p.alpha = __ldg(M + a.maps_plane);
+  if (a.maps_mask & 4) p.ris = __ldg(M + 2 * a.maps_plane);
+}
 
 struct ColArgs {
   void* A;
@@ -350,7 +365,11 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
       else
         v = load_vp<T>(a.V, a.flags, vb + j * TPL, ps.vs);
     }
-    cpx<T> y = nl_point<T, two>(x[j], as, ao, ps, has_v, v);
+    NLP<T> pm = ps;
+    if constexpr (!two) {
+      if (a.flags & F_MAPS) apply_maps<T>(pm, a, f, pix0 + j * TPL);
+    }
+    cpx<T> y = nl_point<T, two>(x[j], as, ao, pm, has_v, v);
     if (two && rabi) {
       // kernels_gpu.py:154-156: A1' = cos*A1 - i*sin*A2, A2' = cos*A2 - i*sin*A1
       const cpx<T> vo = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, po.vs) : mk<T>(T(0), T(0));

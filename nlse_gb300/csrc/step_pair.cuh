@@ -100,19 +100,22 @@ __device__ __forceinline__ cp2 nl_pair_point(cp2 x, const NLP2& p, bool has_v, f
   return {fnma2(x.im, ci, mul2(x.re, cr)), fma2(x.re, ci, mul2(x.im, cr))};
 }
 
-// Shape of the pair row pass: PPC line pairs per CTA (at least 128 threads).
-template <int N>
+// Shape of the pair row pass: EP positions per thread and line (16, or 8 for
+// twice the threads on the same shared memory), PPC line pairs per CTA (at
+// least 128 threads).
+template <int N, int EP = 16>
 struct RowPair {
-  static constexpr int E = Shape<N>::E, TPL = N / E;
+  static constexpr int E = Shape<N, EP>::E, TPL = N / E;
   static constexpr int PPC = TPL >= 128 ? 1 : 128 / TPL;
   static constexpr int LPC = 2 * PPC;
   static constexpr int THREADS = PPC * TPL;
   static constexpr int SLS = stage_len<float>(padded_len(N));
 };
 
-template <int N>
+template <int N, int EP = 16>
 __host__ __device__ constexpr size_t rows_pair_smem() {
-  return (size_t)2 * RowPair<N>::LPC * RowPair<N>::SLS * sizeof(float2) + kRowStages * sizeof(uint64_t);
+  return (size_t)2 * RowPair<N, EP>::LPC * RowPair<N, EP>::SLS * sizeof(float2) +
+         kRowStages * sizeof(uint64_t);
 }
 
 // Persistent inverse row pass on pairs of lines of the blocked spectral
@@ -120,10 +123,11 @@ __host__ __device__ constexpr size_t rows_pair_smem() {
 // and exchange buffers; every wait bounded).
 // VSHARED: the potential is real and both lines of every pair read the same
 // row of it (one potential for the batch and an even number of fields).
-template <int N, int MODE, bool VSHARED>
-__global__ void __launch_bounds__(RowPair<N>::THREADS) k_rows_pair_tma(
+// (three CTAs per SM fit in shared memory: registers are capped to match)
+template <int N, int EP, int MODE, bool VSHARED>
+__global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
     const StepArgs a, const __grid_constant__ CUtensorMap tmS) {
-  using RP = RowPair<N>;
+  using RP = RowPair<N, EP>;
   using C = float2;
   constexpr int E = RP::E, TPL = RP::TPL, W = BlkW<float>::W, NB = N / W, LPC = RP::LPC,
                 SLS = RP::SLS;
@@ -134,7 +138,7 @@ __global__ void __launch_bounds__(RowPair<N>::THREADS) k_rows_pair_tma(
   static_assert(padded_len(N) * sizeof(float4) <= 2 * SLS * sizeof(C),
                 "a pair's exchange fits in its two staging lines");
   constexpr int NEX = fft_exchanges(N, E);
-  static_assert(NEX == 1 || NEX == 2, "one or two exchanges per transform");
+  static_assert(NEX >= 1 && NEX <= 3, "one to three exchanges per transform");
   extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * SLS);
@@ -222,9 +226,21 @@ __global__ void __launch_bounds__(RowPair<N>::THREADS) k_rows_pair_tma(
     for (int j = 0; j < E; ++j) x[j] = {mul2(x[j].re, sc), mul2(x[j].im, sc)};
     // V' = vscale * V rounded in single precision, as the reference's k/2*V array
     auto nl_all = [&](int set) {
-      const NLP2 p = load_nlp2(P, fa, fb, set);
+      const NLP2 p0 = load_nlp2(P, fa, fb, set);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
+        NLP2 p = p0;
+        if (a.flags & F_MAPS) {
+          // per-pixel g, alpha/2, 1/Isat' planes replace the per-field values
+          const float* M = reinterpret_cast<const float*>(a.maps);
+          const int64_t ia = fa * a.maps_fstride + ma * (int64_t)N + t + j * TPL;
+          const int64_t ib = fb * a.maps_fstride + mb * (int64_t)N + t + j * TPL;
+          if (a.maps_mask & 1) p.gs = f2(__ldg(M + ia), __ldg(M + ib));
+          if (a.maps_mask & 2)
+            p.nalpha = f2(-__ldg(M + a.maps_plane + ia), -__ldg(M + a.maps_plane + ib));
+          if (a.maps_mask & 4)
+            p.ris = f2(__ldg(M + 2 * a.maps_plane + ia), __ldg(M + 2 * a.maps_plane + ib));
+        }
         if (!has_v) {
           x[j] = nl_pair_point(x[j], p, false, f2s(0.f), f2s(0.f));
         } else if constexpr (VSHARED) {
@@ -243,7 +259,7 @@ __global__ void __launch_bounds__(RowPair<N>::THREADS) k_rows_pair_tma(
     if (!(a.flags & F_NO_POST)) nl_all(0);
     if constexpr (MODE == ROW_INV_NL_FWD) {
       if (a.flags & F_PRE_NL) nl_all(1);
-      pfft_hook<N, E, false, true, NEX == 1>(x, t, sA, 1, tw, [&] {
+      pfft_hook<N, E, false, true, NEX % 2 == 1>(x, t, sA, 1, tw, [&] {
         if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
       });
       if (act) {
@@ -285,27 +301,39 @@ namespace nlse {
 // (element i of pair p at padi(i) * 2 + p, float4).  Forward column FFT,
 // propagator, inverse column FFT; the propagator (blocked, complex64) values
 // of the tile are requested before the forward transform.
-template <int N>
+// the transform's twiddles in shared memory when they fit
+template <int N, int EP>
+__host__ __device__ constexpr bool cols_pair_tws() {
+  return cols_tma_base_smem<float, N>() + (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) +
+             16 <= kMaxSmemBytes;
+}
+template <int N, int EP = 16>
 __host__ __device__ constexpr size_t cols_pair_smem() {
-  return cols_tma_smem<float, N>();
+  return cols_tma_base_smem<float, N>() +
+         (cols_pair_tws<N, EP>() ? (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) + 16
+                                 : 0);
 }
 
-template <int N>
-__global__ void __launch_bounds__(2 * (N / Shape<N>::E), 1) k_cols_pair_tma(const ColArgs a) {
+template <int N, int EP>
+__global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(const ColArgs a) {
   using C = float2;
-  constexpr int E = Shape<N>::E, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
+  constexpr int E = Shape<N, EP>::E, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
   constexpr int SLW = stage_len<float>(padded_len(N) * W);
   static_assert((SLW * sizeof(C)) % 128 == 0, "bulk copies need aligned shared destinations");
   static_assert(padded_len(N) * 2 * sizeof(float4) <= SLW * sizeof(C),
                 "both pairs' exchanges fit in one staging tile");
   constexpr unsigned TILE_BYTES = TILE * sizeof(C);
+  // Exchanges alternate between the staging tile just read (A) and the
+  // exchange tile (B): the forward transform starts in A, the inverse one in
+  // B when the count is odd, so the inverse transform always ends in B and
+  // A can be refilled right after it.
   constexpr int NEX = fft_exchanges(N, E);
-  constexpr bool DB = NEX > 0 && NEX % 2 == 0;
+  constexpr bool DB = NEX > 0;
   extern __shared__ __align__(128) unsigned char smraw[];
   C* stage = reinterpret_cast<C*>(smraw);
   C* xch = stage + kColStages * SLW;
   uint64_t* bar = reinterpret_cast<uint64_t*>(xch + SLW);
-  constexpr bool TWS = cols_tma_tws<float, N>();
+  constexpr bool TWS = cols_pair_tws<N, EP>();
   C* twc = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(bar) + 16);
   if constexpr (TWS) load_tw_compact<float, N, E>(twc, reinterpret_cast<const C*>(a.tw));
   const C* tw = TWS ? twc : reinterpret_cast<const C*>(a.tw);
@@ -386,7 +414,7 @@ __global__ void __launch_bounds__(2 * (N / Shape<N>::E), 1) k_cols_pair_tma(cons
       x[j] = {fnma2(x[j].im, pi, mul2(x[j].re, pr)), fma2(x[j].re, pi, mul2(x[j].im, pr))};
     }
     if constexpr (DB) {
-      pfft_db<N, E, 1, true, 0, 1, TWS>(x, t, sA, sB, 2, tw);
+      pfft_db<N, E, 1, true, NEX % 2, 1, TWS>(x, t, sA, sB, 2, tw);
       if (threadIdx.x == 0) refill(st, i);
     } else {
       pfft_rest<N, E, 1, true, false, TWS>(x, t, sB, 2, tw);

@@ -107,8 +107,8 @@ class Plan:
                                                   *[ct.byref(x) for x in m]), "kernel variant")
         return {"rows": v[0].value, "cols": v[1].value, "rows_cap": v[2].value,
                 "cols_cap": v[3].value,
-                "rows_avail": [i for i in range(3) if m[0].value >> i & 1],
-                "cols_avail": [i for i in range(3) if m[1].value >> i & 1]}
+                "rows_avail": [i for i in range(4) if m[0].value >> i & 1],
+                "cols_avail": [i for i in range(4) if m[1].value >> i & 1]}
 
     def get_kernels(self) -> tuple:
         """(rows_tma, cols_tma, rows_tma available, cols_tma available)."""
@@ -156,6 +156,8 @@ class OperatorData:
     prop_cstride: int = 0
     pump: tuple | None = None  # (pump_r, pump_t, probe_r, probe_t) device tensors or None
     nl_khat: torch.Tensor | None = None  # nonlocal kernel spectrum on the padded grid
+    maps: torch.Tensor | None = None  # [3][map fields][pixels] g, alpha/2, 1/Isat' planes
+    maps_mask: int = 0
     keep: list = field(default_factory=list)
     # unique per operator: tells the plan its cached copy of the propagator is stale
     version: int = field(default_factory=lambda: next(_versions))
@@ -182,6 +184,11 @@ class OperatorData:
         o.prop_version = int(self.version)
         if self.nl_khat is not None:
             o.nl_khat = self.nl_khat.data_ptr()
+        if self.maps is not None and self.maps_mask:
+            o.nl_maps = self.maps.data_ptr()
+            o.maps_plane = int(self.maps.shape[1] * self.maps.shape[2])
+            o.maps_fstride = int(self.maps.shape[2]) if self.maps.shape[1] > 1 else 0
+            o.maps_mask = int(self.maps_mask)
         return o
 
 
@@ -318,6 +325,35 @@ def per_field(x, lead: tuple, n_axes: int, name: str) -> np.ndarray:
     except ValueError:
         raise ValueError(f"{name} of shape {np.shape(x)} does not broadcast to fields {lead}") from None
     return np.ascontiguousarray(b).reshape(-1)
+
+
+def varies_on_grid(x, n_axes: int) -> bool:
+    """Whether a parameter, broadcast with NumPy's rules against fields whose
+    last n_axes axes are the grid, changes along a grid axis (its own trailing
+    n_axes dimensions, right-aligned, are not all 1)."""
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().numpy()
+    shape = np.shape(x)
+    tail = shape[max(0, len(shape) - n_axes):]
+    return any(t != 1 for t in tail)
+
+
+def coef_plane(x, lead: tuple, grid: tuple) -> np.ndarray:
+    """A grid-varying parameter broadcast to the fields: (1, pixels) when it is
+    the same for every field, else (fields, pixels); float64."""
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().numpy()
+    a = np.asarray(x, dtype=np.float64)
+    full = tuple(lead) + tuple(grid)
+    try:
+        b = np.broadcast_to(a, full)
+    except ValueError:
+        raise ValueError(f"parameter of shape {a.shape} does not broadcast to fields {full}") from None
+    pix = int(np.prod(grid))
+    own_lead = a.shape[:max(0, a.ndim - len(grid))]
+    if all(s == 1 for s in own_lead):
+        return np.ascontiguousarray(b.reshape(-1, pix)[:1])
+    return np.ascontiguousarray(b).reshape(-1, pix)
 
 
 def next_pow2(n: int) -> int:

@@ -298,9 +298,12 @@ class NLSE:
         na = len(self._last_axes)
         P = np.zeros((nf, _lib.NLSE_PARAM_STRIDE), dtype=np.float64)
         dz = self.delta_z
-        g = engine.per_field(self.k / 2 * _host(self.n2) * c * epsilon_0, lead, na, "n2")
-        alpha = engine.per_field(_host(self.alpha) / 2, lead, na, "alpha")
-        isat = engine.per_field(2 * _host(self.I_sat) / (epsilon_0 * c), lead, na, "Isat")
+        # a coefficient that varies over the grid goes to a plane (_coef_planes);
+        # its per-field slot is then not read
+        cg, ca, ci = self._nl_coefs()
+        g = 0.0 if engine.varies_on_grid(cg, na) else engine.per_field(cg, lead, na, "n2")
+        alpha = 0.0 if engine.varies_on_grid(ca, na) else engine.per_field(ca, lead, na, "alpha")
+        isat = np.inf if engine.varies_on_grid(ci, na) else engine.per_field(ci, lead, na, "Isat")
         vs = self.k / 2
         for s, dzs in ((0, dz / 2 if precision == "double" else dz), (1, dz / 2)):
             o = s * 16
@@ -313,6 +316,38 @@ class NLSE:
             P[:, o + 5] = np.inf
             P[:, o + 6] = vs
         return P
+
+    def _nl_coefs(self) -> tuple:
+        """The nonlinear step's coefficients as the reference forms them for
+        nl_prop (nlse.py:411-428): g = k/2 n2 c eps0, alpha/2, Isat' = 2 Isat/(eps0 c),
+        scalars or arrays that broadcast against the field."""
+        return (self.k / 2 * _host(self.n2) * c * epsilon_0, _host(self.alpha) / 2,
+                2 * _host(self.I_sat) / (epsilon_0 * c))
+
+    def _coef_planes(self, lead: tuple, grid: tuple, real_dtype, dev) -> tuple:
+        """Planes [3][map fields][pixels] (g, alpha/2, 1/Isat') of the coefficients
+        that vary over the grid -- the reference broadcasts n2, alpha and Isat
+        arrays elementwise in nl_prop (nlse.py:309-328, kernels_gpu.py:4-65) --
+        and the mask of the planes present; (None, 0) when none does."""
+        na = len(self._last_axes)
+        planes, mask = [None, None, None], 0
+        for i, x in enumerate(self._nl_coefs()):
+            if engine.varies_on_grid(x, na):
+                if self._comps != 1:
+                    raise NotImplementedError("coefficients varying over the grid are "
+                                              "supported for one-component fields")
+                p = engine.coef_plane(x, lead, grid)
+                planes[i] = 1.0 / p if i == 2 else p
+                mask |= 1 << i
+        if not mask:
+            return None, 0
+        nmf = max(p.shape[0] for p in planes if p is not None)
+        pix = int(np.prod(grid))
+        out = np.zeros((3, nmf, pix), dtype=np.float64)
+        for i, p in enumerate(planes):
+            if p is not None:
+                out[i] = np.broadcast_to(p, (nmf, pix))
+        return torch.from_numpy(out).to(device=dev, dtype=real_dtype), mask
 
     def _prop_layout(self, prop: torch.Tensor) -> int:
         """Element stride between the components' propagators (0: shared)."""
@@ -357,10 +392,12 @@ class NLSE:
             plan.set_nonlocal(pads)
         else:
             plan.set_nonlocal(None)
+        maps, mask = self._coef_planes(lead, tuple(A.shape[-na:]), A.real.dtype, dev)
         return OperatorData(prop=prop.contiguous(), params=params,
                             scheme=1 if precision == "double" else 0,
                             rabi=self._rabi_enabled(precision), V=Vd, v_fstride=vstride,
-                            prop_cstride=self._prop_layout(prop), pump=pump, nl_khat=khat)
+                            prop_cstride=self._prop_layout(prop), pump=pump, nl_khat=khat,
+                            maps=maps, maps_mask=mask)
 
     def _rabi_enabled(self, precision: str) -> bool:
         return False

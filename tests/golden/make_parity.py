@@ -16,6 +16,8 @@ Parts (each writes .npz files under tests/golden/):
             FFTs -> short/<case>.npz {out, out_numpy, out_torch, steps}.
   ddgpe128  the four DDGPE cases with complex128 fields -> ddgpe_c128_<branch>.npz
             (replayed by the golden tests like every other fixture).
+  maps      NLSE 2-D with n2, alpha and Isat varying over the grid -> maps_*.npz
+            (golden fixtures; run before spread and short, which cover them).
   fullsize  the benchmark configurations at their stated sizes (outputs
             subsampled on a regular grid, FP64 power of the whole field):
               nlse2048   2048^2 noisy beam, dz = 2e-5 m, 501 steps, "single":
@@ -155,6 +157,36 @@ def part_ddgpe128() -> None:
         save(HERE / f"ddgpe_c128_{branch}.npz", **arrays)
 
 
+def part_maps() -> None:
+    """NLSE 2-D with n2, alpha and Isat varying over the grid (the reference
+    broadcasts them in nl_prop; float64 arrays make it evaluate the step in
+    FP64), 64^2, 201 steps: complex64 "single" and complex128 "double", and a
+    three-field batch with a per-field n2 and an Isat map."""
+    from tests import golden_cases as gc
+
+    use_fft("scipy")
+    N = 64
+    sim = _R.NLSE(mg.ALPHA, mg.POWER, mg.WINDOW, mg.N2, None, mg.L, NX=N, NY=N, Isat=mg.ISAT,
+                  backend="GPU")
+    XX, YY = sim.XX.astype(np.float64), sim.YY.astype(np.float64)
+    n2 = mg.N2 * (1 + 0.5 * np.exp(-(XX ** 2 + YY ** 2) / (1.5e-3) ** 2))
+    alpha = mg.ALPHA * (1 + 0.5 * XX / mg.WINDOW)
+    isat = mg.ISAT * (1 + 4 * (YY / mg.WINDOW) ** 2)
+    E = mg.gauss(sim.XX, sim.YY)
+    V = mg.well(sim.XX, sim.YY).astype(np.complex64)
+    for name, dt, prec, B in (("maps_c64_single", np.complex64, "single", 0),
+                              ("maps_c128_double", np.complex128, "double", 0),
+                              ("maps_c64_batch3", np.complex64, "single", 3)):
+        E_in = (np.broadcast_to(E, (B, N, N)) if B else E).astype(dt)
+        f = dict(E_in=E_in, V=V,
+                 n2=n2 if not B else np.linspace(-1.6e-9, -4e-10, B).reshape(B, 1, 1),
+                 alpha=alpha if not B else np.asarray(mg.ALPHA), isat=isat,
+                 precision=np.array(prec))
+        np.savez_compressed(HERE / f"{name}.npz", **f, out=np.zeros(0))
+        out = gc.run(name, "reference")
+        save(HERE / f"{name}.npz", **f, out=out)
+
+
 # ---------------------------------------------------------------------------
 # full-size configurations
 # ---------------------------------------------------------------------------
@@ -185,7 +217,11 @@ def mixed_inputs(R_NLSE, dtype, group: int):
 
 
 def part_fullsize(which=("nlse2048", "cnlse1024", "mixed")) -> None:
-    R = _R
+    from functools import partial
+    from types import SimpleNamespace
+
+    # the reference's GPU path (its constructors pick the CPU backend by default here)
+    R = SimpleNamespace(NLSE=partial(_R.NLSE, backend="GPU"), CNLSE=partial(_R.CNLSE, backend="GPU"))
     if "nlse2048" in which:
         for dtype, kinds in ((np.complex128, ("scipy",)), (np.complex64, ("scipy", "numpy", "torch"))):
             outs = {}
@@ -243,7 +279,7 @@ _R = None
 
 def main() -> None:
     global _R
-    parts = [a for a in sys.argv[1:] if a in ("spread", "short", "ddgpe128", "fullsize")
+    parts = [a for a in sys.argv[1:] if a in ("spread", "short", "ddgpe128", "maps", "fullsize")
              or a.startswith("fullsize:")]
     args = [a for a in sys.argv[1:] if a not in parts]
     sys.argv = [sys.argv[0]] + args
@@ -256,9 +292,11 @@ def main() -> None:
 
     gc.set_reference(_R)
     print(f"reference NLSE {_R.__version__} from {ref}")
-    for part in parts or ["spread", "short", "ddgpe128", "fullsize"]:
+    for part in parts or ["maps", "spread", "short", "ddgpe128", "fullsize"]:
         t = time.time()
-        if part == "spread":
+        if part == "maps":
+            part_maps()
+        elif part == "spread":
             part_spread()
         elif part == "short":
             part_short()

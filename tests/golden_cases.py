@@ -94,6 +94,15 @@ def run(name: str, kind: str, upcast: bool = False, steps: int | None = None):
         sim.delta_z = float(dz)
         sim.V = None if f["V"].size == 0 else f["V"].copy()
         return _out(kind, sim, E, _z(float(z), float(dz), steps), str(f["precision"]))
+    if name.startswith("maps"):
+        # n2, alpha, Isat as arrays over the grid (or per field), set after construction
+        sim = C["NLSE"](ALPHA, POWER, WINDOW, N2, None, L, NX=64, NY=64, Isat=ISAT)
+        sim.n2 = f["n2"] if f["n2"].ndim else f["n2"][()]
+        sim.alpha = f["alpha"] if f["alpha"].ndim else f["alpha"][()]
+        sim.I_sat = f["isat"] if f["isat"].ndim else f["isat"][()]
+        sim.delta_z = 5e-5
+        sim.V = f["V"].copy()
+        return _out(kind, sim, E, _z(L, 5e-5, steps), str(f["precision"]))
     if name.startswith("nlse1d"):
         sim = C["NLSE_1d"](ALPHA, POWER, WINDOW, N2, None, L, NX=256, Isat=ISAT)
         sim.delta_z = 5e-5

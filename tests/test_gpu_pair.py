@@ -60,10 +60,12 @@ def test_pair_passes_match_scalar_passes_and_oracle(NY, NX, B, vmode, dz, scheme
     z = (STEPS - 0.5) * abs(dz)
     plan = engine.Plan.get(2, (NY, NX), B, 1, _lib.NLSE_C64, torch.device("cuda", 0))
     avail = plan.get_variant()
-    assert _lib.ROWS_PAIR in avail["rows_avail"] and _lib.COLS_PAIR in avail["cols_avail"]
+    assert {_lib.ROWS_PAIR, _lib.ROWS_PAIR8} <= set(avail["rows_avail"])
+    assert {_lib.COLS_PAIR, _lib.COLS_PAIR8} <= set(avail["cols_avail"])
     outs = {}
     for v in ((_lib.ROWS_PAIR, _lib.COLS_PAIR), (_lib.ROWS_TMA, _lib.COLS_TMA),
-              (_lib.ROWS_PAIR, _lib.COLS_TMA), (_lib.ROWS_TMA, _lib.COLS_PAIR)):
+              (_lib.ROWS_PAIR, _lib.COLS_TMA), (_lib.ROWS_TMA, _lib.COLS_PAIR),
+              (_lib.ROWS_PAIR8, _lib.COLS_PAIR8), (_lib.ROWS_PAIR8, _lib.COLS_PAIR)):
         plan.set_variant(*v)
         outs[v] = p.out_field(E, z, precision=scheme, verbose=False)
         plan.status()

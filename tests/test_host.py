@@ -129,6 +129,39 @@ def test_per_field_broadcasting():
         engine.per_field(np.ones((2, 1, 1)), (3,), 2, "n2")
 
 
+def test_grid_varying_coefficients_become_planes():
+    """n2, alpha and Isat arrays over the grid (the reference broadcasts them in
+    nl_prop) become per-pixel planes g, alpha/2, 1/Isat'; per-field and scalar
+    ones stay in the parameter block."""
+    import torch
+
+    assert not engine.varies_on_grid(np.ones((3, 1, 1)), 2)
+    assert engine.varies_on_grid(np.ones((16,)), 2)          # broadcasts along x
+    assert engine.varies_on_grid(np.ones((16, 1)), 2)        # along y
+    assert engine.coef_plane(np.arange(4.0), (3,), (2, 4)).shape == (1, 8)
+    assert engine.coef_plane(np.ones((3, 2, 4)), (3,), (2, 4)).shape == (3, 8)
+    N = 16
+    n2map = -1.6e-9 * (1 + 0.1 * np.arange(N * N).reshape(N, N) / (N * N))
+    isat = np.full((N, N), 1e5)
+    isat[:, : N // 2] = 2e5
+    # (a grid-shaped n2 with a (B,) power does not broadcast in the reference's
+    # default-step expression either; the power stays scalar here)
+    s = ng.NLSE(20, 1.0, 8.92e-3, n2map, None, 1e-2, NX=N, NY=N, Isat=isat)
+    s.alpha = np.full((2, 1, 1), 20.0)                        # per field: stays in the block
+    s.delta_z = 5e-5
+    P = s._nl_block((2,), "single", False)
+    assert np.all(P[:, 1] == 10.0) and np.all(P[:, 4] == np.inf) and np.all(P[:, 2] == 0.0)
+    maps, mask = s._coef_planes((2,), (N, N), torch.float64, "cpu")
+    assert mask == 0b101 and tuple(maps.shape) == (3, 1, N * N)
+    g = s.k / 2 * n2map * c * epsilon_0
+    np.testing.assert_array_equal(maps[0, 0].numpy(), g.reshape(-1))
+    np.testing.assert_array_equal(maps[2, 0].numpy(), (1 / (2 * isat / (epsilon_0 * c))).reshape(-1))
+    # two-component fields keep the error
+    cn = ng.CNLSE(20, 1.0, 8.92e-3, n2map, -1e-10, None, 1e-2, NX=N, NY=N, Isat=1e5)
+    with pytest.raises(NotImplementedError):
+        cn._nl_block((), "single", False)
+
+
 def test_nlse_parameter_block_formulas():
     s = ng.NLSE(20, 1.05, 8.92e-3, -1.6e-9, None, 1e-2, NX=16, NY=16, Isat=1e5)
     s.delta_z = 5e-5
