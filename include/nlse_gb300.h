@@ -146,14 +146,20 @@ int nlse_propagate(nlse_plan plan, void* A, const nlse_operator* op, int64_t nst
                    int64_t step0, int32_t flags, void* stream);
 
 /*
- * Groups of fields with different geometries advanced together: each group
- * (its own plan, field and operator) runs its nsteps[i] split steps on a
- * branch of one CUDA graph, the branches concurrent, so the whole batched
- * z-loop is one graph launch (replayed when called again with the same
- * arguments; NLSE_RUN_GRAPH is implied).  A batch of mixed grids (e.g.
+ * Groups of fields with different geometries advanced together, the whole
+ * batched z-loop one CUDA graph launch (replayed when called again with the
+ * same arguments; NLSE_RUN_GRAPH is implied).  A batch of mixed grids (e.g.
  * 96 fields at 256^2, 48 at 512^2, 16 at 1024^2, 4 at 2048^2) is four
- * groups.  No reference counterpart as one call: the reference runs
- * one out_field per NLSE instance.
+ * groups, each with its own plan, field and operator.
+ * When every group is a one-component complex64 2-D field of 256..2048
+ * points per axis with the TMA row pass, the same step count, no nonlocal
+ * response or pump terms and a complex64 propagator (and at most 8 groups),
+ * each step is TWO launches for the whole batch: one persistent column pass
+ * over every group's tiles and one persistent row pass over every group's
+ * lines (after each group's first forward row pass); NLSE_GROUP_FUSED=0
+ * turns this off.  Otherwise each group runs its own step sequence on a
+ * concurrent branch of the graph.  No reference counterpart as one call: the
+ * reference runs one out_field per NLSE instance.
  */
 typedef struct nlse_group_s* nlse_group;
 int nlse_group_create(nlse_group* out);
@@ -161,6 +167,9 @@ int nlse_group_destroy(nlse_group group);
 int nlse_group_propagate(nlse_group group, int32_t ngroups, const nlse_plan* plans,
                          void* const* fields, const nlse_operator* ops, const int64_t* nsteps,
                          void* stream);
+/* 1 if the group's last nlse_group_propagate ran two launches per step for the
+ * whole batch, 0 if it ran one branch per group. */
+int nlse_group_fused(nlse_group group);
 
 /* Kernel variants of a plan's 2-D passes: TMA-fed persistent row passes
  * (rows_tma) or one CTA per line, TMA-fed persistent column passes (cols_tma)

@@ -36,6 +36,9 @@ SOURCES = [
     "rows_pair8_mid.cu",
     "rows_pair8_last.cu",
     "cols_pair.cu",
+    "multi_pair.cu",
+    "multi_rows_mid.cu",
+    "multi_rows_last.cu",
     "fno.cu",
 ]
 
@@ -91,7 +94,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
 
     jobs = jobs or min(len(SOURCES), os.cpu_count() or 4)
     # longest translation units first
-    order = sorted(SOURCES, key=lambda s: (not s.startswith("rows"), s))
+    order = sorted(SOURCES, key=lambda s: (not s.startswith(("rows", "multi_rows")), s))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(compile_one, order))
     tmp = out.with_suffix(".so.tmp")

@@ -81,6 +81,7 @@ SIGNATURES = [
      + [ct.POINTER(ct.c_uint32)] * 2),
     ("nlse_group_create", ct.c_int, [ct.POINTER(ct.c_void_p)]),
     ("nlse_group_destroy", ct.c_int, [ct.c_void_p]),
+    ("nlse_group_fused", ct.c_int, [ct.c_void_p]),
     (
         "nlse_group_propagate",
         ct.c_int,

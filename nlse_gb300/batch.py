@@ -2,9 +2,11 @@
 
 The reference runs one out_field per NLSE instance; a mixed batch (fields of
 different grid sizes, powers, n2 and potentials) is several instances.
-out_fields takes such a list and advances every instance's z-loop as one
-branch of a single CUDA graph (nlse_group_propagate), the branches running
-concurrently on the GPU.  Each instance keeps its own plan (scratch) for
+out_fields takes such a list and advances every instance's z-loop in one
+CUDA graph (nlse_group_propagate): for one-component complex64 grids of
+256..2048 points per axis, two launches per step for the whole batch (one
+column pass over every instance's tiles, one row pass over every instance's
+lines); otherwise one concurrent branch of the graph per instance.  Each instance keeps its own plan (scratch) for
 this.  Callbacks are not available here (use out_field per instance).
 """
 
@@ -37,6 +39,8 @@ class _Group:
 
 
 _group = None
+# whether the last out_fields ran the whole batch as two launches per step
+last_fused = False
 
 
 def _own_plan(simu, A: torch.Tensor) -> Plan:
@@ -89,6 +93,8 @@ def out_fields(jobs, z: float, precision: str = "single", normalize: bool = True
             _lib.check(_group.lib.nlse_group_propagate(_group.handle, n, plans, fields, ops, steps,
                                                        engine.stream_handle(dev)),
                        "group propagate")
+        global last_fused
+        last_fused = bool(_group.lib.nlse_group_fused(_group.handle))
     finally:
         for item in prepared:
             item[0].n2 = item[6]

@@ -755,6 +755,77 @@ int nlse_plan_destroy(nlse_plan p) {
 
 }  // extern "C"
 
+namespace {
+
+// Whether a group runs as one launch per pass per step (step_multi.cuh):
+// complex64 one-component 2-D plans of 256..2048 points per axis with the TMA
+// row pass, the same number of steps, no nonlocal response or pump terms, a
+// complex64 propagator; NLSE_GROUP_FUSED=0 turns it off.
+bool group_fused_ok(int n, const nlse_plan* plans, const nlse_operator* ops,
+                    const int64_t* nsteps) {
+  const char* env = getenv("NLSE_GROUP_FUSED");
+  if (env && env[0] == '0') return false;
+  if (n < 1 || n > multi_max_plans()) return false;
+  for (int i = 0; i < n; ++i) {
+    const nlse_plan_s* p = plans[i];
+    const nlse_operator* op = &ops[i];
+    const nlse_desc& d = p->d;
+    if (nsteps[i] != nsteps[0] || nsteps[i] < 1) return false;
+    if (d.dtype != NLSE_C64 || d.comps != 1 || d.ndim != 2 || !p->blk || !p->rows_tma_ok)
+      return false;
+    if (p->lg[0] < 8 || p->lg[0] > 11 || p->lg[1] < 8 || p->lg[1] > 11) return false;
+    if (op->nl_khat || op->pump_r || op->probe_r || op->prop_c128) return false;
+    if (d.nfields * d.shape[0] >= (int64_t(1) << 31)) return false;
+  }
+  return true;
+}
+
+// The whole batch's loop with two launches per step (columns of every plan,
+// then rows of every plan), after each plan's parameter mirror, propagator
+// layout and first forward row pass.
+int enqueue_group_fused(int n, const nlse_plan* plans, void* const* fields,
+                        const nlse_operator* ops, int64_t nsteps, cudaStream_t s) {
+  std::vector<StepArgs> mid(n), last(n);
+  std::vector<ColArgs> col(n);
+  std::vector<const CUtensorMap*> tm(n);
+  std::vector<int> lr(n), lc(n);
+  for (int i = 0; i < n; ++i) {
+    nlse_plan_s* p = plans[i];
+    const nlse_operator* op = &ops[i];
+    int rc = mirror_params(p, op, s);
+    if (rc == NLSE_OK) rc = refresh_prop(p, op, false, s);
+    if (rc != NLSE_OK) return rc;
+    StepArgs a = row_args(p, fields[i], op);
+    a.tma_grid = p->nsm;
+    const uint32_t pre = op->scheme == 1 ? F_PRE_NL : 0u;
+    StepArgs a0 = a;
+    a0.flags |= pre | F_OUT_BLK;
+    cudaError_t e = rows(p, ROW_FWD, p->lg[1], a0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "row pass (forward)");
+    mid[i] = a;
+    mid[i].flags |= pre | F_IN_BLK | F_OUT_BLK;
+    last[i] = a;
+    last[i].flags |= F_IN_BLK;
+    col[i] = col_blk_args(p, op);
+    tm[i] = &p->tmS;
+    lr[i] = p->lg[1];
+    lc[i] = p->lg[0];
+  }
+  const int nsm = plans[0]->nsm;
+  for (int64_t st = 0; st < nsteps; ++st) {
+    cudaError_t e = launch_cols_multi(n, col.data(), lc.data(), nsm, s, false);
+    if (e != cudaSuccess) return cuda_fail(e, "column pass (all plans)");
+    if (st + 1 < nsteps)
+      e = launch_rows_multi(ROW_INV_NL_FWD, n, mid.data(), tm.data(), lr.data(), nsm, s, false);
+    else
+      e = launch_rows_multi(ROW_INV_NL, n, last.data(), tm.data(), lr.data(), nsm, s, false);
+    if (e != cudaSuccess) return cuda_fail(e, "row pass (all plans)");
+  }
+  return NLSE_OK;
+}
+
+}  // namespace
+
 struct nlse_group_s {
   cudaStream_t cap = nullptr;
   std::vector<cudaStream_t> branch;
@@ -762,6 +833,7 @@ struct nlse_group_s {
   cudaEvent_t fork = nullptr;
   cudaGraphExec_t gexec = nullptr;
   std::vector<uint8_t> key;  // serialized arguments of the captured graph
+  int fused = 0;             // the captured graph runs two launches per step for the batch
 };
 
 extern "C" {
@@ -772,6 +844,9 @@ int nlse_group_create(nlse_group* out) {
   auto* g = new nlse_group_s();
   cudaError_t e = cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  // kernel attributes of the one-launch-per-pass kernels (outside any capture)
+  if (e == cudaSuccess) e = launch_rows_multi(0, 0, nullptr, nullptr, nullptr, 0, nullptr, true);
+  if (e == cudaSuccess) e = launch_cols_multi(0, nullptr, nullptr, 0, nullptr, true);
   if (e != cudaSuccess) {
     nlse_group_destroy(g);
     return cuda_fail(e, "group create");
@@ -815,7 +890,29 @@ int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* 
   put(ops, sizeof(nlse_operator) * n);
   put(nsteps, sizeof(int64_t) * n);
   for (int i = 0; i < n; ++i) put(&plans[i]->kgen, sizeof(uint64_t));
+  const uint8_t fused = group_fused_ok(n, plans, ops, nsteps) ? 1 : 0;
+  put(&fused, 1);
+  g->fused = fused;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (fused && !(g->gexec && key == g->key)) {
+    cudaGraph_t graph = nullptr;
+    NLSE_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const int rc = enqueue_group_fused(n, plans, fields, ops, nsteps[0], g->cap);
+    const cudaError_t e2 = cudaStreamEndCapture(g->cap, &graph);
+    if (rc != NLSE_OK || e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      if (rc != NLSE_OK) return rc;
+      return cuda_fail(e2, "group capture");
+    }
+    if (g->gexec) {
+      cudaGraphExecDestroy(g->gexec);
+      g->gexec = nullptr;
+    }
+    const cudaError_t e = cudaGraphInstantiate(&g->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "group graph instantiate");
+    g->key = key;
+  }
   if (!(g->gexec && key == g->key)) {
     while ((int)g->branch.size() < n) {
       cudaStream_t st;
@@ -855,6 +952,8 @@ int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* 
   NLSE_CUDA(cudaGraphLaunch(g->gexec, s), "group graph launch");
   return NLSE_OK;
 }
+
+int nlse_group_fused(nlse_group g) { return g ? g->fused : 0; }
 
 int nlse_plan_status(nlse_plan p, void* stream) {
   g_err.clear();

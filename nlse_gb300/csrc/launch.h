@@ -35,6 +35,17 @@ cudaError_t launch_rows_pair(int mode, int log2n, const StepArgs& a, bool vshare
 cudaError_t launch_cols_pair(int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only,
                              int cap_per_sm, int ep);
 
+// One launch per pass over several plans (step_multi.cuh): complex64
+// one-component 2-D plans of 256..2048 points per axis with TMA row passes.
+// Rows: mode ROW_INV_NL or ROW_INV_NL_FWD, each plan's step arguments (on the
+// blocked buffer) and tensor map.  Columns: each plan's blocked column
+// arguments.  nsm: SMs of the device.  prepare_only: set kernel attributes.
+int multi_max_plans();
+cudaError_t launch_rows_multi(int mode, int n, const StepArgs* a, const CUtensorMap* const* tm,
+                              const int* log2n, int nsm, cudaStream_t s, bool prepare_only);
+cudaError_t launch_cols_multi(int n, const ColArgs* c, const int* log2n, int nsm, cudaStream_t s,
+                              bool prepare_only);
+
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction
 int64_t noalloc_partials_max();     // capacity of the static partial-sum array

@@ -1,0 +1,273 @@
+// One persistent launch per pass for a batch of plans with different grids.
+//
+// A mixed batch (e.g. 96 fields at 256^2, 48 at 512^2, 16 at 1024^2 and 4 at
+// 2048^2) is several plans; these kernels advance all of them in one launch
+// per pass.  The work of every plan is one list of items:
+//   k_rows_pair_multi  item = the LPC pixel-lines of one pair row-pass group
+//                      of one plan (128 threads and the same 2 x 34.8 KB of
+//                      shared memory at every grid size from 256 to 2048);
+//   k_cols_pair_multi  item = 2048/N column tiles of one plan, side by side
+//                      (256 threads: 2 * N/16 per tile; the same 3 x 69.6 KB
+//                      of shared memory at every size).
+// Persistent CTAs take items blockIdx.x, blockIdx.x + gridDim.x, ...; the next
+// item's copies (possibly another plan's) are issued while the current item
+// is transformed, as in the single-plan pair passes (step_pair.cuh), whose
+// arithmetic this is: pair_row_item is shared, the column item repeats
+// k_cols_pair_tma's body per tile.  Every wait is bounded.
+#pragma once
+#include "step_pair.cuh"
+
+namespace nlse {
+
+constexpr int kMultiMax = 8;      // plans per launch
+constexpr int kMultiLog2Min = 8;  // grids of 256 ...
+constexpr int kMultiLog2Max = 11; // ... to 2048 points per axis
+
+// Row-pass buffer of one stage: LPC lines of SLS elements, the same for
+// every N in [256, 2048] with 16 positions per thread.
+constexpr int kMultiRowHalf = 2 * RowPair<2048>::SLS;
+static_assert(RowPair<256>::LPC * RowPair<256>::SLS == kMultiRowHalf &&
+                  RowPair<512>::LPC * RowPair<512>::SLS == kMultiRowHalf &&
+                  RowPair<1024>::LPC * RowPair<1024>::SLS == kMultiRowHalf,
+              "row-pass stage buffers of every grid size have one length");
+
+struct RowPlanArgs {
+  StepArgs a;       // the plan's step arguments (F_IN_BLK, out flags, parameters)
+  unsigned items;   // its line groups
+  unsigned item0;   // index of its first item in the launch's list
+  int log2n;        // row length
+};
+
+struct __align__(64) RowMulti {
+  CUtensorMap tm[kMultiMax];  // each plan's tensor map of its blocked buffer
+  RowPlanArgs p[kMultiMax];
+  int nplans;
+  unsigned items;
+};
+
+__host__ __device__ constexpr size_t rows_multi_smem() {
+  return (size_t)2 * kMultiRowHalf * sizeof(float2) + kRowStages * sizeof(uint64_t);
+}
+
+__device__ __forceinline__ int multi_plan_of(unsigned item, const unsigned* item0, int n) {
+  int k = 0;
+  while (k + 1 < n && item >= item0[k + 1]) ++k;
+  return k;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constant__ RowMulti m) {
+  using C = float2;
+  constexpr int W = BlkW<float>::W;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* X = reinterpret_cast<C*>(smraw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * kMultiRowHalf);
+  __shared__ unsigned s_item0[kMultiMax];
+  if (threadIdx.x < kMultiMax) s_item0[threadIdx.x] = threadIdx.x < m.nplans ? m.p[threadIdx.x].item0 : 0xffffffffu;
+  // copies of item `item` into stage b (thread 0)
+  auto issue = [&](int b, unsigned item) {
+    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const RowPlanArgs& P = m.p[k];
+    const int N = 1 << P.log2n;
+    const int TPL = N / 16, PPC = TPL >= 128 ? 1 : 128 / TPL, LPC = 2 * PPC;
+    const int SLS = padded_len(N);  // stage_len of a padded line: a multiple of 16 here
+    const int NB = N / W, BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
+    const unsigned nq = (unsigned)P.a.nq, nf = nq / (unsigned)P.a.lines_per_comp;
+    const unsigned q0 = (item - P.item0) * LPC;
+    const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+    mbar_arrive_expect_tx(&bar[b], nl * (unsigned)N * (unsigned)sizeof(C));
+    for (unsigned l = 0; l < nl; ++l) {
+      const unsigned q = q0 + l, f = q % nf, y = q / nf;
+      for (int bx = 0; bx < NBOX; ++bx)
+        tensor_load_4d(X + b * kMultiRowHalf + l * SLS + bx * BOXB * W, &m.tm[k], 0, (int)y,
+                       bx * BOXB, (int)f, &bar[b]);
+    }
+  };
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kRowStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x < m.items) issue(0, blockIdx.x);
+  int it = 0;
+  for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
+    const int st = it & 1;
+    const unsigned par = (it >> 1) & 1;
+    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const StepArgs& a = m.p[k].a;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+      }
+      return;
+    }
+    const unsigned g = item - m.p[k].item0, next = item + gridDim.x;
+    C* Xs = X + st * kMultiRowHalf;
+    C* Xn = X + (st ^ 1) * kMultiRowHalf;
+    auto prefetch = [&] {
+      if (next < m.items) {
+        fence_proxy_async_smem();
+        issue(st ^ 1, next);
+      }
+    };
+    switch (m.p[k].log2n) {
+      case 8: pair_row_item<256, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
+      case 9: pair_row_item<512, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
+      case 10: pair_row_item<1024, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
+      default: pair_row_item<2048, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
+    }
+  }
+}
+
+// ---- column pass ------------------------------------------------------------
+constexpr int kMultiColTile = stage_len<float>(padded_len(2048) * BlkW<float>::W);  // one stage
+
+struct ColPlanArgs {
+  ColArgs c;      // the plan's blocked column arguments (S, blocked propagator)
+  unsigned items; // its items (2048/N tiles each)
+  unsigned item0;
+  int log2n;      // column length
+};
+
+struct ColMulti {
+  ColPlanArgs p[kMultiMax];
+  int nplans;
+  unsigned items;
+};
+
+__host__ __device__ constexpr size_t cols_multi_smem() {
+  return (size_t)(kColStages + 1) * kMultiColTile * sizeof(float2) + kColStages * sizeof(uint64_t);
+}
+
+// One item of the column pass: sub = 2048/N tiles, tile s handled by threads
+// [s * 2 TPL, (s + 1) * 2 TPL); the same arithmetic as k_cols_pair_tma.
+// Returns after refilling stage st (thread 0 calls refill()).
+template <int N, typename Refill>
+__device__ __forceinline__ void pair_col_item(const ColArgs& c, unsigned g, float2* stage_st,
+                                              float2* xch, Refill&& refill) {
+  using C = float2;
+  constexpr int E = 16, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
+  constexpr int SLW = stage_len<float>(padded_len(N) * W), SUB = 2048 / N;
+  static_assert(SLW * SUB == kMultiColTile, "sub-tiles fill one stage");
+  constexpr int NEX = fft_exchanges(N, E);
+  static_assert(NEX >= 1, "column transforms exchange at least once");
+  const int s = threadIdx.x / (2 * TPL), lt = threadIdx.x % (2 * TPL);
+  const int p = lt & 1, t = lt >> 1;
+  const int64_t nouter = c.nblocks / c.ncb;
+  const int64_t ti = (int64_t)g * SUB + s;
+  const bool act = ti < c.nblocks;
+  const int64_t tc = act ? ti : c.nblocks - 1;
+  const int64_t o = tc % nouter, b = tc / nouter;
+  const C* tw = reinterpret_cast<const C*>(c.tw);
+  cp2 x[E];
+  {
+    const float4* sp = reinterpret_cast<const float4*>(stage_st + s * SLW) + t * 2 + p;
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float4 v = sp[j * TPL * 2];
+      x[j] = {f2(v.x, v.z), f2(v.y, v.w)};
+    }
+  }
+  const int64_t toff = b * (int64_t)TILE + (int64_t)t * W + 2 * p;
+  const int64_t pb = (o % c.comps) * c.prop_cstride + toff;
+  float4 pre[E];
+#pragma unroll
+  for (int j = 0; j < E; ++j)
+    pre[j] = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const C*>(c.prop) + pb +
+                                                   (int64_t)j * TPL * W));
+  __syncthreads();  // every thread has read the stage
+  float4* sA = reinterpret_cast<float4*>(stage_st + s * SLW) + p;
+  float4* sB = reinterpret_cast<float4*>(xch + s * SLW) + p;
+  pfft_db<N, E, 1, false, 0, 1, false>(x, t, sA, sB, 2, tw);
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float2 pr = f2(pre[j].x, pre[j].z), pi = f2(pre[j].y, pre[j].w);
+    x[j] = {fnma2(x[j].im, pi, mul2(x[j].re, pr)), fma2(x[j].re, pi, mul2(x[j].im, pr))};
+  }
+  pfft_db<N, E, 1, true, NEX % 2, 1, false>(x, t, sA, sB, 2, tw);
+  if (threadIdx.x == 0) refill();
+  if (act) {
+    float4* gp = reinterpret_cast<float4*>(reinterpret_cast<C*>(c.A) + o * c.outer_stride + toff);
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      gp[(int64_t)j * TPL * 2] = make_float4(x[j].re.x, x[j].im.x, x[j].re.y, x[j].im.y);
+  }
+}
+
+// (a template so that only the translation unit that launches it compiles it)
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(256, 1) k_cols_pair_multi(const __grid_constant__ ColMulti m) {
+  using C = float2;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* stage = reinterpret_cast<C*>(smraw);
+  C* xch = stage + kColStages * kMultiColTile;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + kMultiColTile);
+  __shared__ unsigned s_item0[kMultiMax];
+  if (threadIdx.x < kMultiMax) s_item0[threadIdx.x] = threadIdx.x < m.nplans ? m.p[threadIdx.x].item0 : 0xffffffffu;
+  // bulk copies of item `item` (its tiles side by side) into stage st (thread 0)
+  auto issue = [&](int st, unsigned item) {
+    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const ColArgs& c = m.p[k].c;
+    const int N = 1 << m.p[k].log2n, SUB = 2048 / N;
+    const int SLW = kMultiColTile / SUB;
+    const unsigned tile_bytes = (unsigned)N * BlkW<float>::W * (unsigned)sizeof(C);
+    const int64_t nouter = c.nblocks / c.ncb;
+    const int64_t t0 = (int64_t)(item - m.p[k].item0) * SUB;
+    int nt = 0;
+    for (int s = 0; s < SUB; ++s) nt += (t0 + s < c.nblocks);
+    mbar_arrive_expect_tx(&bar[st], nt * tile_bytes);
+    for (int s = 0; s < SUB; ++s) {
+      const int64_t ti = t0 + s;
+      if (ti >= c.nblocks) break;
+      const C* src = reinterpret_cast<const C*>(c.A) + (ti % nouter) * c.outer_stride +
+                     (ti / nouter) * (int64_t)N * BlkW<float>::W;
+      bulk_load(stage + st * kMultiColTile + s * SLW, src, tile_bytes, &bar[st]);
+    }
+  };
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int st = 0; st < kColStages; ++st) {
+      const unsigned i = blockIdx.x + (unsigned)st * gridDim.x;
+      if (i < m.items) issue(st, i);
+    }
+  int it = 0;
+  for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
+    const int st = it % kColStages;
+    const unsigned par = (it / kColStages) & 1;
+    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const ColArgs& c = m.p[k].c;
+    const bool ok = mbar_wait_bounded(&bar[st], par);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(c.status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&bar[st], par);
+        if (item + gridDim.x < m.items)
+          mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kColStages) & 1);
+      }
+      return;
+    }
+    const unsigned g = item - m.p[k].item0;
+    const unsigned next = item + (unsigned)kColStages * gridDim.x;
+    auto refill = [&] {
+      if (next < m.items) {
+        fence_proxy_async_smem();
+        issue(st, next);
+      }
+    };
+    C* sst = stage + st * kMultiColTile;
+    switch (m.p[k].log2n) {
+      case 8: pair_col_item<256>(c, g, sst, xch, refill); break;
+      case 9: pair_col_item<512>(c, g, sst, xch, refill); break;
+      case 10: pair_col_item<1024>(c, g, sst, xch, refill); break;
+      default: pair_col_item<2048>(c, g, sst, xch, refill); break;
+    }
+  }
+}
+
+}  // namespace nlse

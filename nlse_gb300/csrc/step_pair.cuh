@@ -118,6 +118,128 @@ __host__ __device__ constexpr size_t rows_pair_smem() {
          kRowStages * sizeof(uint64_t);
 }
 
+// One work item of the pair row pass: LPC consecutive pixel-lines (PPC pairs),
+// already in shared memory buffer Xs (line l at Xs + l * SLS); Xn is the other
+// buffer (the second exchange buffer).  prefetch() is run by thread 0 once
+// every read of Xn is complete, to refill it.  g: the item's index.
+template <int N, int EP, int MODE, bool VSHARED, typename Prefetch>
+__device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, float2* Xs,
+                                              float2* Xn, Prefetch&& prefetch) {
+  using RP = RowPair<N, EP>;
+  using C = float2;
+  constexpr int E = RP::E, TPL = RP::TPL, W = BlkW<float>::W, LPC = RP::LPC, SLS = RP::SLS;
+  constexpr int NEX = fft_exchanges(N, E);
+  static_assert(NEX >= 1 && NEX <= 3, "one to three exchanges per transform");
+  static_assert(padded_len(N) * sizeof(float4) <= 2 * SLS * sizeof(C),
+                "a pair's exchange fits in its two staging lines");
+  const int pp = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  const unsigned nq = (unsigned)a.nq;
+  const unsigned nf = nq / (unsigned)a.lines_per_comp;
+  auto q_f = [&](unsigned q) { return q % nf; };
+  auto q_y = [&](unsigned q) { return q / nf; };
+  auto buf = [&](C* B, int l) { return B + l * SLS; };
+  const float2* tw = reinterpret_cast<const float2*>(a.tw);
+  const float* P = a.params_f32;
+  const bool has_v = a.flags & F_HAS_V;
+  const bool v_cplx = a.flags & F_V_COMPLEX;
+  const float2 sc = f2s(a.inv_nf);
+  // pairs past the end (last group) compute on in-range lines and store nothing
+  const unsigned qa = g * LPC + 2 * pp;
+  const bool act = qa + 1 < nq;
+  const unsigned qca = act ? qa : nq - 2, qcb = qca + 1;
+  const int64_t fa = q_f(qca), ma = q_y(qca), fb = q_f(qcb), mb = q_y(qcb);
+  cp2 x[E];
+  {
+    const C* la = buf(Xs, 2 * pp);
+    const C* lb = buf(Xs, 2 * pp + 1);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const C u = la[t + j * TPL], v = lb[t + j * TPL];
+      x[j] = {f2(u.x, v.x), f2(u.y, v.y)};
+    }
+  }
+  // potential: VSHARED (both lines read the same row of one shared real
+  // potential) prefetches one value per position before the transform;
+  // otherwise each lane's value is read when the nonlinear step needs it
+  const int64_t va = fa * a.v_fstride + ma * (int64_t)N + t;
+  const int64_t vb = fb * a.v_fstride + mb * (int64_t)N + t;
+  float vpre[VSHARED ? E : 1];
+  if constexpr (VSHARED) {
+    if (has_v) {
+      const float* V1 = reinterpret_cast<const float*>(a.V);
+#pragma unroll
+      for (int j = 0; j < E; ++j) vpre[j] = __ldg(V1 + va + j * TPL);
+    }
+  }
+  __syncthreads();  // every thread has read its lines from buffer st
+  float4* sA = reinterpret_cast<float4*>(buf(Xs, 2 * pp));
+  float4* sB = reinterpret_cast<float4*>(buf(Xn, 2 * pp));
+  pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
+#pragma unroll
+  for (int j = 0; j < E; ++j) x[j] = {mul2(x[j].re, sc), mul2(x[j].im, sc)};
+  // V' = vscale * V rounded in single precision, as the reference's k/2*V array
+  auto nl_all = [&](int set) {
+    const NLP2 p0 = load_nlp2(P, fa, fb, set);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      NLP2 p = p0;
+      if (a.flags & F_MAPS) {
+        // per-pixel g, alpha/2, 1/Isat' planes replace the per-field values
+        const float* M = reinterpret_cast<const float*>(a.maps);
+        const int64_t ia = fa * a.maps_fstride + ma * (int64_t)N + t + j * TPL;
+        const int64_t ib = fb * a.maps_fstride + mb * (int64_t)N + t + j * TPL;
+        if (a.maps_mask & 1) p.gs = f2(__ldg(M + ia), __ldg(M + ib));
+        if (a.maps_mask & 2)
+          p.nalpha = f2(-__ldg(M + a.maps_plane + ia), -__ldg(M + a.maps_plane + ib));
+        if (a.maps_mask & 4)
+          p.ris = f2(__ldg(M + 2 * a.maps_plane + ia), __ldg(M + 2 * a.maps_plane + ib));
+      }
+      if (!has_v) {
+        x[j] = nl_pair_point(x[j], p, false, f2s(0.f), f2s(0.f));
+      } else if constexpr (VSHARED) {
+        x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2s(vpre[j])), f2s(0.f));
+      } else if (v_cplx) {
+        const float2* V2 = reinterpret_cast<const float2*>(a.V);
+        const float2 u = __ldg(V2 + va + j * TPL), w = __ldg(V2 + vb + j * TPL);
+        x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2(u.x, w.x)), mul2(p.vs, f2(u.y, w.y)));
+      } else {
+        const float* V1 = reinterpret_cast<const float*>(a.V);
+        const float2 u = f2(__ldg(V1 + va + j * TPL), __ldg(V1 + vb + j * TPL));
+        x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, u), f2s(0.f));
+      }
+    }
+  };
+  if (!(a.flags & F_NO_POST)) nl_all(0);
+  if constexpr (MODE == ROW_INV_NL_FWD) {
+    if (a.flags & F_PRE_NL) nl_all(1);
+    pfft_hook<N, E, false, true, NEX % 2 == 1>(x, t, sA, 1, tw, [&] {
+      if (threadIdx.x == 0) prefetch();
+    });
+    if (act) {
+      const int64_t lpc = a.lines_per_comp, dstr = (int64_t)TPL * lpc;
+      C* da = reinterpret_cast<C*>(a.S) + fa * a.pix + ((t / W) * lpc + ma) * W + (t % W);
+      C* db = reinterpret_cast<C*>(a.S) + fb * a.pix + ((t / W) * lpc + mb) * W + (t % W);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        da[j * dstr] = f2(x[j].re.x, x[j].im.x);
+        db[j * dstr] = f2(x[j].re.y, x[j].im.y);
+      }
+    }
+  } else {
+    __syncthreads();  // B is no longer read
+    if (threadIdx.x == 0) prefetch();
+    if (act) {
+      C* da = reinterpret_cast<C*>(a.A) + fa * a.pix + ma * N + t;
+      C* db = reinterpret_cast<C*>(a.A) + fb * a.pix + mb * N + t;
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        da[j * TPL] = f2(x[j].re.x, x[j].im.x);
+        db[j * TPL] = f2(x[j].re.y, x[j].im.y);
+      }
+    }
+  }
+}
+
 // Persistent inverse row pass on pairs of lines of the blocked spectral
 // buffer (the k_rows_tma schedule: two line buffers alternate as TMA staging
 // and exchange buffers; every wait bounded).
@@ -129,21 +251,15 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
     const StepArgs a, const __grid_constant__ CUtensorMap tmS) {
   using RP = RowPair<N, EP>;
   using C = float2;
-  constexpr int E = RP::E, TPL = RP::TPL, W = BlkW<float>::W, NB = N / W, LPC = RP::LPC,
-                SLS = RP::SLS;
+  constexpr int W = BlkW<float>::W, NB = N / W, LPC = RP::LPC, SLS = RP::SLS;
   constexpr int BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
   constexpr unsigned ROW_BYTES = N * sizeof(C);
   static_assert((SLS * sizeof(C)) % 128 == 0 && (BOXB * W * sizeof(C)) % 128 == 0,
                 "tensor-map copies need 128-byte aligned shared destinations");
-  static_assert(padded_len(N) * sizeof(float4) <= 2 * SLS * sizeof(C),
-                "a pair's exchange fits in its two staging lines");
-  constexpr int NEX = fft_exchanges(N, E);
-  static_assert(NEX >= 1 && NEX <= 3, "one to three exchanges per transform");
   extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * SLS);
   auto buf = [&](int b, int l) { return X + (b * LPC + l) * SLS; };
-  const int pp = threadIdx.x / TPL, t = threadIdx.x % TPL;
   const unsigned nq = (unsigned)a.nq;
   const unsigned ngroups = (nq + LPC - 1) / LPC;
   const unsigned nf = nq / (unsigned)a.lines_per_comp;
@@ -166,12 +282,6 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
       issue(b, gn);
     }
   };
-  const float2* tw = reinterpret_cast<const float2*>(a.tw);
-  const float* P = a.params_f32;
-  const bool has_v = a.flags & F_HAS_V;
-  const bool v_cplx = a.flags & F_V_COMPLEX;
-  const float2 sc = f2s(a.inv_nf);
-
   if (threadIdx.x == 0) {
     for (int st = 0; st < kRowStages; ++st) mbar_init(&bar[st], 1);
     mbar_init_fence();
@@ -190,101 +300,9 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
       }
       return;
     }
-    // pairs past the end (last group) compute on in-range lines and store nothing
-    const unsigned qa = g * LPC + 2 * pp;
-    const bool act = qa + 1 < nq;
-    const unsigned qca = act ? qa : nq - 2, qcb = qca + 1;
-    const int64_t fa = q_f(qca), ma = q_y(qca), fb = q_f(qcb), mb = q_y(qcb);
-    cp2 x[E];
-    {
-      const C* la = buf(st, 2 * pp);
-      const C* lb = buf(st, 2 * pp + 1);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        const C u = la[t + j * TPL], v = lb[t + j * TPL];
-        x[j] = {f2(u.x, v.x), f2(u.y, v.y)};
-      }
-    }
-    // potential: VSHARED (both lines read the same row of one shared real
-    // potential) prefetches one value per position before the transform;
-    // otherwise each lane's value is read when the nonlinear step needs it
-    const int64_t va = fa * a.v_fstride + ma * (int64_t)N + t;
-    const int64_t vb = fb * a.v_fstride + mb * (int64_t)N + t;
-    float vpre[VSHARED ? E : 1];
-    if constexpr (VSHARED) {
-      if (has_v) {
-        const float* V1 = reinterpret_cast<const float*>(a.V);
-#pragma unroll
-        for (int j = 0; j < E; ++j) vpre[j] = __ldg(V1 + va + j * TPL);
-      }
-    }
-    __syncthreads();  // every thread has read its lines from buffer st
-    float4* sA = reinterpret_cast<float4*>(buf(st, 2 * pp));
-    float4* sB = reinterpret_cast<float4*>(buf(st ^ 1, 2 * pp));
-    pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
-#pragma unroll
-    for (int j = 0; j < E; ++j) x[j] = {mul2(x[j].re, sc), mul2(x[j].im, sc)};
-    // V' = vscale * V rounded in single precision, as the reference's k/2*V array
-    auto nl_all = [&](int set) {
-      const NLP2 p0 = load_nlp2(P, fa, fb, set);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        NLP2 p = p0;
-        if (a.flags & F_MAPS) {
-          // per-pixel g, alpha/2, 1/Isat' planes replace the per-field values
-          const float* M = reinterpret_cast<const float*>(a.maps);
-          const int64_t ia = fa * a.maps_fstride + ma * (int64_t)N + t + j * TPL;
-          const int64_t ib = fb * a.maps_fstride + mb * (int64_t)N + t + j * TPL;
-          if (a.maps_mask & 1) p.gs = f2(__ldg(M + ia), __ldg(M + ib));
-          if (a.maps_mask & 2)
-            p.nalpha = f2(-__ldg(M + a.maps_plane + ia), -__ldg(M + a.maps_plane + ib));
-          if (a.maps_mask & 4)
-            p.ris = f2(__ldg(M + 2 * a.maps_plane + ia), __ldg(M + 2 * a.maps_plane + ib));
-        }
-        if (!has_v) {
-          x[j] = nl_pair_point(x[j], p, false, f2s(0.f), f2s(0.f));
-        } else if constexpr (VSHARED) {
-          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2s(vpre[j])), f2s(0.f));
-        } else if (v_cplx) {
-          const float2* V2 = reinterpret_cast<const float2*>(a.V);
-          const float2 u = __ldg(V2 + va + j * TPL), w = __ldg(V2 + vb + j * TPL);
-          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, f2(u.x, w.x)), mul2(p.vs, f2(u.y, w.y)));
-        } else {
-          const float* V1 = reinterpret_cast<const float*>(a.V);
-          const float2 u = f2(__ldg(V1 + va + j * TPL), __ldg(V1 + vb + j * TPL));
-          x[j] = nl_pair_point(x[j], p, true, mul2(p.vs, u), f2s(0.f));
-        }
-      }
-    };
-    if (!(a.flags & F_NO_POST)) nl_all(0);
-    if constexpr (MODE == ROW_INV_NL_FWD) {
-      if (a.flags & F_PRE_NL) nl_all(1);
-      pfft_hook<N, E, false, true, NEX % 2 == 1>(x, t, sA, 1, tw, [&] {
-        if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
-      });
-      if (act) {
-        const int64_t lpc = a.lines_per_comp, dstr = (int64_t)TPL * lpc;
-        C* da = reinterpret_cast<C*>(a.S) + fa * a.pix + ((t / W) * lpc + ma) * W + (t % W);
-        C* db = reinterpret_cast<C*>(a.S) + fb * a.pix + ((t / W) * lpc + mb) * W + (t % W);
-#pragma unroll
-        for (int j = 0; j < E; ++j) {
-          da[j * dstr] = f2(x[j].re.x, x[j].im.x);
-          db[j * dstr] = f2(x[j].re.y, x[j].im.y);
-        }
-      }
-    } else {
-      __syncthreads();  // B is no longer read
-      if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
-      if (act) {
-        C* da = reinterpret_cast<C*>(a.A) + fa * a.pix + ma * N + t;
-        C* db = reinterpret_cast<C*>(a.A) + fb * a.pix + mb * N + t;
-#pragma unroll
-        for (int j = 0; j < E; ++j) {
-          da[j * TPL] = f2(x[j].re.x, x[j].im.x);
-          db[j * TPL] = f2(x[j].re.y, x[j].im.y);
-        }
-      }
-    }
+    pair_row_item<N, EP, MODE, VSHARED>(a, g, buf(st, 0), buf(st ^ 1, 0), [&] {
+      prefetch(st ^ 1, g + gridDim.x);
+    });
   }
 }
 

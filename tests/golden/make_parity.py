@@ -14,7 +14,8 @@ Parts (each writes .npz files under tests/golden/):
             rounding changes.
   short     every complex64 case stopped after 20 loop steps, with all three
             FFTs -> short/<case>.npz {out, out_numpy, out_torch, steps}.
-  ddgpe128  the four DDGPE cases with complex128 fields -> ddgpe_c128_<branch>.npz
+  ddgpe128  the four DDGPE cases with complex128 fields and pump profiles
+            -> ddgpe_c128_<branch>.npz
             (replayed by the golden tests like every other fixture).
   maps      NLSE 2-D with n2, alpha and Isat varying over the grid -> maps_*.npz
             (golden fixtures; run before spread and short, which cover them).
@@ -145,16 +146,23 @@ def part_short() -> None:
 
 
 def part_ddgpe128() -> None:
+    """The DDGPE cases with complex128 fields and complex128 pump and probe
+    profiles: the reference forms the pump term F_r * F_t[i] * dz * 1j in the
+    profiles' precision, so complex128 profiles keep the whole step in FP64."""
     gc, _ = _cases()
     use_fft("scipy")
     for branch in ("single_noV", "single_V", "double_noV", "double_V"):
         src = gc.load(f"ddgpe_c64_{branch}")
-        out = gc.run(f"ddgpe_c64_{branch}", "reference", upcast=True)
-        assert out.dtype == np.complex128
         arrays = dict(src)
         arrays["E_in"] = src["E_in"].astype(np.complex128)
+        for k in ("Fr", "Ft", "Pr", "Pt"):
+            arrays[k] = src[k].astype(np.complex128)
+        name = f"ddgpe_c128_{branch}"
+        np.savez_compressed(HERE / f"{name}.npz", **{**arrays, "out": np.zeros(0)})
+        out = gc.run(name, "reference")
+        assert out.dtype == np.complex128
         arrays["out"] = out
-        save(HERE / f"ddgpe_c128_{branch}.npz", **arrays)
+        save(HERE / f"{name}.npz", **arrays)
 
 
 def part_maps() -> None:
