@@ -965,8 +965,11 @@ int nlse_plan_status(nlse_plan p, void* stream) {
   if (h != DEV_OK) {
     NLSE_CUDA(cudaMemsetAsync(p->status, 0, sizeof(int), s), "status reset");
     NLSE_CUDA(cudaStreamSynchronize(s), "status sync");
-    return fail(NLSE_ERR_TIMEOUT, "a bounded wait inside a kernel gave up (device code %d); the "
-                "results of the calls since the last status check are not valid", h);
+    return fail(NLSE_ERR_TIMEOUT, "a kernel stopped early (device code %d: %s); the results of "
+                "the calls since the last status check are not valid", h,
+                h == DEV_WAIT_TIMEOUT ? "a bounded wait gave up"
+                : h == DEV_SMEM_MISALIGNED ? "shared memory not 128-byte aligned for its copies"
+                                           : "unknown");
   }
   return NLSE_OK;
 }

@@ -435,7 +435,7 @@ template <typename T, int N, int E, int MODE, int NC>
 __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a) {
   using C = cpx<T>;
   constexpr int TPL = RowCfg<N, E>::TPL, LPB = RowCfg<N, E>::LPB, SL = RowCfg<N, E>::SL;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int lb = threadIdx.x / TPL, t = threadIdx.x % TPL;
@@ -580,6 +580,10 @@ __global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
   extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * NC * SLS);
+  if (!smem_base_aligned(X)) {  // tensor-map copies need a 128-byte aligned destination
+    if (threadIdx.x == 0) atomicExch(a.status, DEV_SMEM_MISALIGNED);
+    return;
+  }
   auto buf = [&](int b, int li, int cc) { return X + ((b * LPC + li) * NC + cc) * SLS; };
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int li = threadIdx.x / (NC * TPL);
@@ -711,7 +715,7 @@ template <typename T, int N, int E, int MODE, bool PC128>
 __global__ void __launch_bounds__(kColMaxThreads) k_cols(const ColArgs a) {
   using C = cpx<T>;
   constexpr int TPL = N / E;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int W = a.w;
@@ -741,7 +745,7 @@ template <typename T, int N, int E, int MODE, bool PC128>
 __global__ void __launch_bounds__(BlkW<T>::W * (N / E)) k_cols_blk(const ColArgs a) {
   using C = cpx<T>;
   constexpr int TPL = N / E, W = BlkW<T>::W;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int c = threadIdx.x % W, t = threadIdx.x / W;

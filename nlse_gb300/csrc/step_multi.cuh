@@ -49,9 +49,11 @@ __host__ __device__ constexpr size_t rows_multi_smem() {
   return (size_t)2 * kMultiRowHalf * sizeof(float2) + kRowStages * sizeof(uint64_t);
 }
 
-__device__ __forceinline__ int multi_plan_of(unsigned item, const unsigned* item0, int n) {
+// Plan of a work item (the plans' items follow each other in the list).
+template <typename M>
+__device__ __forceinline__ int multi_plan_of(unsigned item, const M& m) {
   int k = 0;
-  while (k + 1 < n && item >= item0[k + 1]) ++k;
+  while (k + 1 < m.nplans && item >= m.p[k + 1].item0) ++k;
   return k;
 }
 
@@ -62,11 +64,13 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
   extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * kMultiRowHalf);
-  __shared__ unsigned s_item0[kMultiMax];
-  if (threadIdx.x < kMultiMax) s_item0[threadIdx.x] = threadIdx.x < m.nplans ? m.p[threadIdx.x].item0 : 0xffffffffu;
+  if (!smem_base_aligned(X)) {  // tensor-map copies need a 128-byte aligned destination
+    if (threadIdx.x == 0 && m.nplans > 0) atomicExch(m.p[0].a.status, DEV_SMEM_MISALIGNED);
+    return;
+  }
   // copies of item `item` into stage b (thread 0)
   auto issue = [&](int b, unsigned item) {
-    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const int k = multi_plan_of(item, m);
     const RowPlanArgs& P = m.p[k];
     const int N = 1 << P.log2n;
     const int TPL = N / 16, PPC = TPL >= 128 ? 1 : 128 / TPL, LPC = 2 * PPC;
@@ -93,7 +97,7 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
   for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
     const int st = it & 1;
     const unsigned par = (it >> 1) & 1;
-    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const int k = multi_plan_of(item, m);
     const StepArgs& a = m.p[k].a;
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
@@ -204,11 +208,13 @@ __global__ void __launch_bounds__(256, 1) k_cols_pair_multi(const __grid_constan
   C* stage = reinterpret_cast<C*>(smraw);
   C* xch = stage + kColStages * kMultiColTile;
   uint64_t* bar = reinterpret_cast<uint64_t*>(xch + kMultiColTile);
-  __shared__ unsigned s_item0[kMultiMax];
-  if (threadIdx.x < kMultiMax) s_item0[threadIdx.x] = threadIdx.x < m.nplans ? m.p[threadIdx.x].item0 : 0xffffffffu;
+  if (!smem_base_aligned(stage)) {
+    if (threadIdx.x == 0 && m.nplans > 0) atomicExch(m.p[0].c.status, DEV_SMEM_MISALIGNED);
+    return;
+  }
   // bulk copies of item `item` (its tiles side by side) into stage st (thread 0)
   auto issue = [&](int st, unsigned item) {
-    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const int k = multi_plan_of(item, m);
     const ColArgs& c = m.p[k].c;
     const int N = 1 << m.p[k].log2n, SUB = 2048 / N;
     const int SLW = kMultiColTile / SUB;
@@ -240,7 +246,7 @@ __global__ void __launch_bounds__(256, 1) k_cols_pair_multi(const __grid_constan
   for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
     const int st = it % kColStages;
     const unsigned par = (it / kColStages) & 1;
-    const int k = multi_plan_of(item, s_item0, m.nplans);
+    const int k = multi_plan_of(item, m);
     const ColArgs& c = m.p[k].c;
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {

@@ -259,6 +259,10 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
   extern __shared__ __align__(128) unsigned char smraw[];
   C* X = reinterpret_cast<C*>(smraw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(X + 2 * LPC * SLS);
+  if (!smem_base_aligned(X)) {  // tensor-map copies need a 128-byte aligned destination
+    if (threadIdx.x == 0) atomicExch(a.status, DEV_SMEM_MISALIGNED);
+    return;
+  }
   auto buf = [&](int b, int l) { return X + (b * LPC + l) * SLS; };
   const unsigned nq = (unsigned)a.nq;
   const unsigned ngroups = (nq + LPC - 1) / LPC;

@@ -8,7 +8,7 @@
 namespace nlse {
 
 // Error codes a kernel may record in the plan's status word.
-enum : int { DEV_OK = 0, DEV_WAIT_TIMEOUT = 1 };
+enum : int { DEV_OK = 0, DEV_WAIT_TIMEOUT = 1, DEV_SMEM_MISALIGNED = 2 };
 
 // A wait gives up after this many nanoseconds of the global timer.
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
@@ -60,6 +60,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
 // Polls after which a wait gives up even if the timer should not advance
 // (each poll is a try_wait, which may itself suspend for a while).
 constexpr unsigned kWaitMaxPolls = 1u << 26;
+
+// Whether a kernel's dynamic shared memory starts on the 128-byte boundary
+// its tensor-map copies need (every thread; the caller records a failure
+// and returns before issuing any copy when it does not).
+__device__ __forceinline__ bool smem_base_aligned(const void* p) { return (smem_addr(p) & 127u) == 0; }
 
 // Wait for phase `parity` of the barrier; false if limit_ns passed first.
 __device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, unsigned parity,
