@@ -79,6 +79,7 @@ cudaError_t launch_mul_spectrum(int dtype, void* X, const void* K, int64_t per, 
                                 cudaStream_t s);
 cudaError_t launch_nl_pointwise_pad(int dtype, const StepArgs& a, const void* X, int64_t ny,
                                     int64_t nx, int64_t py, int64_t px, int set, cudaStream_t s);
+// Blocked copy of the propagator, scaled by 1/(ny nx) (exact: a power of two).
 cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_t comps, int64_t ny,
                                int64_t nx, int w, cudaStream_t s);
 

@@ -361,12 +361,15 @@ cudaError_t launch_prop_to_blk(int prop_c128, const void* nat, void* blk, int64_
                                int64_t nx, int w, cudaStream_t s) {
   const int64_t total = comps * ny * nx;
   if (total <= 0) return cudaSuccess;
+  const double scale = 1.0 / (double)(ny * nx);  // a power of two
   if (prop_c128)
     k_prop_to_blk<double><<<grid_for(total, 256), 256, 0, s>>>(
-        reinterpret_cast<const double2*>(nat), reinterpret_cast<double2*>(blk), total, ny, nx, w);
+        reinterpret_cast<const double2*>(nat), reinterpret_cast<double2*>(blk), total, ny, nx, w,
+        scale);
   else
     k_prop_to_blk<float><<<grid_for(total, 256), 256, 0, s>>>(
-        reinterpret_cast<const float2*>(nat), reinterpret_cast<float2*>(blk), total, ny, nx, w);
+        reinterpret_cast<const float2*>(nat), reinterpret_cast<float2*>(blk), total, ny, nx, w,
+        (float)scale);
   return cudaGetLastError();
 }
 

@@ -496,9 +496,12 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS) k_rows(const StepArgs a
       fft_line<T, N, E, 1, false>(x, t, sml, 1, tw);
     } else {
       fft_line<T, N, E, 1, true>(x, t, sml, 1, tw);
-      const T s = inv_n_of<T>(a);
+      // the blocked buffer's column pass applied 1/N already (k_prop_to_blk)
+      if (!(a.flags & F_IN_BLK)) {
+        const T s = inv_n_of<T>(a);
 #pragma unroll
-      for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], s);
+        for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], s);
+      }
       if constexpr (MODE != ROW_INV) {
         if (!(a.flags & F_NO_POST)) {
           if (two) exchange_partner<T, N, E>(x, xo, sm, lb, t);
@@ -660,9 +663,7 @@ __global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
     C* sB = buf(st ^ 1, li, comp);  // second exchange buffer
     C* xpart = buf(st ^ 1, li, 0);  // partner exchange region (NC lines)
     fft_line_db<T, N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
-    const T sc = inv_n_of<T>(a);
-#pragma unroll
-    for (int j = 0; j < E; ++j) x[j] = cscale<T>(x[j], sc);
+    // (1/N: applied by the column pass through the blocked propagator)
     if (!(a.flags & F_NO_POST)) {
       if (two) {
         exchange_partner<T, N, E>(x, xo, xpart, comp, t);
@@ -902,16 +903,20 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E), 1) k_cols_blk_tma(const 
 }
 
 // Natural [comps][NY][NX] propagator -> blocked layout with block width W.
+// The copy carries the inverse 2-D transform's 1/(NY NX), a power of two:
+// the scaling is exact, so the field after the inverse column and row
+// transforms has the same bits as when the row pass scaled it, and the row
+// passes that read the blocked buffer multiply by nothing.
 template <typename TP>
 __global__ void k_prop_to_blk(const cpx<TP>* __restrict__ nat, cpx<TP>* __restrict__ blk,
-                              int64_t total, int64_t ny, int64_t nx, int w) {
+                              int64_t total, int64_t ny, int64_t nx, int w, TP scale) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t pix = ny * nx;
     const int64_t comp = i / pix, r = i % pix;
     const int64_t bx = r / (ny * w), rem = r % (ny * w);
     const int64_t y = rem / w, c = rem % w;
-    blk[i] = nat[comp * pix + y * nx + bx * w + c];
+    blk[i] = cscale<TP>(nat[comp * pix + y * nx + bx * w + c], scale);
   }
 }
 

@@ -31,6 +31,26 @@ static_assert(RowPair<256>::LPC * RowPair<256>::SLS == kMultiRowHalf &&
                   RowPair<1024>::LPC * RowPair<1024>::SLS == kMultiRowHalf,
               "row-pass stage buffers of every grid size have one length");
 
+// Every tensor-map copy of the multi row pass lands on a 128-byte boundary
+// inside its stage buffer: line l < LPC of grid N at stage b goes to
+// b * kMultiRowHalf + l * SLS(N) (+ 256 runs of 32 bytes per box).
+__host__ __device__ constexpr bool multi_row_copies_aligned() {
+  for (int lg = kMultiLog2Min; lg <= kMultiLog2Max; ++lg) {
+    const int N = 1 << lg, TPL = N / 16, PPC = TPL >= 128 ? 1 : 128 / TPL, LPC = 2 * PPC;
+    const int SLS = stage_len<float>(padded_len(N));
+    const int NB = N / 4, BOXB = NB < 256 ? NB : 256;
+    for (int b = 0; b < 2; ++b)
+      for (int l = 0; l < LPC; ++l)
+        for (int bx = 0; bx * BOXB < NB; ++bx) {
+          const long off = ((long)b * kMultiRowHalf + (long)l * SLS + (long)bx * BOXB * 4) * 8;
+          if (off % 128 != 0) return false;
+        }
+    if (LPC * SLS > kMultiRowHalf) return false;
+  }
+  return true;
+}
+static_assert(multi_row_copies_aligned(), "multi row pass: copy destinations aligned and in bounds");
+
 struct RowPlanArgs {
   StepArgs a;       // the plan's step arguments (F_IN_BLK, out flags, parameters)
   unsigned items;   // its line groups
@@ -74,7 +94,9 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
     const RowPlanArgs& P = m.p[k];
     const int N = 1 << P.log2n;
     const int TPL = N / 16, PPC = TPL >= 128 ? 1 : 128 / TPL, LPC = 2 * PPC;
-    const int SLS = padded_len(N);  // stage_len of a padded line: a multiple of 16 here
+    // the line stride pair_row_item reads with: the padded line rounded up to
+    // 128 bytes (every line's tensor-map copy needs a 128-byte aligned destination)
+    const int SLS = stage_len<float>(padded_len(N));
     const int NB = N / W, BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
     const unsigned nq = (unsigned)P.a.nq, nf = nq / (unsigned)P.a.lines_per_comp;
     const unsigned q0 = (item - P.item0) * LPC;

@@ -142,7 +142,6 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
   const float* P = a.params_f32;
   const bool has_v = a.flags & F_HAS_V;
   const bool v_cplx = a.flags & F_V_COMPLEX;
-  const float2 sc = f2s(a.inv_nf);
   // pairs past the end (last group) compute on in-range lines and store nothing
   const unsigned qa = g * LPC + 2 * pp;
   const bool act = qa + 1 < nq;
@@ -175,8 +174,7 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
   float4* sA = reinterpret_cast<float4*>(buf(Xs, 2 * pp));
   float4* sB = reinterpret_cast<float4*>(buf(Xn, 2 * pp));
   pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
-#pragma unroll
-  for (int j = 0; j < E; ++j) x[j] = {mul2(x[j].re, sc), mul2(x[j].im, sc)};
+  // (1/N: applied by the column pass through the blocked propagator)
   // V' = vscale * V rounded in single precision, as the reference's k/2*V array
   auto nl_all = [&](int set) {
     const NLP2 p0 = load_nlp2(P, fa, fb, set);
