@@ -190,6 +190,10 @@ int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
  *   cols: NLSE_COLS_TILE (one CTA per tile), NLSE_COLS_TMA (persistent bulk-
  *         copy ring), NLSE_COLS_PAIR (the ring with two columns per thread in
  *         packed FP32: complex64, columns of 64..2048 points).
+ *   NLSE_ROWS_DEEP / NLSE_COLS_DEEP: the pair passes with deeper prefetch
+ *         (the next work item's copies in flight during the whole current
+ *         item; rows: exchanges in the item's own buffer, columns: three
+ *         staging tiles and no exchange tile), same sizes as the pair ones.
  * rows_ctas_per_sm / cols_ctas_per_sm cap the persistent passes' CTAs per SM
  * (0: as many as fit), which sets their grid (SMs x CTAs per SM).  A launch
  * the chosen variant cannot serve (two components, Rabi or pump terms, a
@@ -203,10 +207,12 @@ int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
 #define NLSE_ROWS_TMA 1
 #define NLSE_ROWS_PAIR 2
 #define NLSE_ROWS_PAIR8 3 /* NLSE_ROWS_PAIR with 8 positions per thread: twice the threads */
+#define NLSE_ROWS_DEEP 4
 #define NLSE_COLS_TILE 0
 #define NLSE_COLS_TMA 1
 #define NLSE_COLS_PAIR 2
 #define NLSE_COLS_PAIR8 3 /* NLSE_COLS_PAIR with 8 positions per thread: twice the threads */
+#define NLSE_COLS_DEEP 4
 int nlse_plan_set_variant(nlse_plan plan, int32_t rows, int32_t cols, int32_t rows_ctas_per_sm,
                           int32_t cols_ctas_per_sm);
 int nlse_plan_get_variant(nlse_plan plan, int32_t* rows, int32_t* cols, int32_t* rows_ctas_per_sm,

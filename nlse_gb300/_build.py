@@ -36,6 +36,9 @@ SOURCES = [
     "rows_pair8_mid.cu",
     "rows_pair8_last.cu",
     "cols_pair.cu",
+    "rows_deep_mid.cu",
+    "rows_deep_last.cu",
+    "cols_deep.cu",
     "multi_pair.cu",
     "multi_rows_mid.cu",
     "multi_rows_last.cu",

@@ -18,8 +18,8 @@ NLSE_RUN_GRAPH = 1
 NLSE_PARAM_STRIDE = 40
 PASS_FORWARD, PASS_LINEAR, PASS_INV_NL_FWD, PASS_INV_NL = 0, 1, 2, 3
 # kernel variants of the 2-D passes (nlse_plan_set_variant)
-ROWS_LINE, ROWS_TMA, ROWS_PAIR, ROWS_PAIR8 = 0, 1, 2, 3
-COLS_TILE, COLS_TMA, COLS_PAIR, COLS_PAIR8 = 0, 1, 2, 3
+ROWS_LINE, ROWS_TMA, ROWS_PAIR, ROWS_PAIR8, ROWS_DEEP = 0, 1, 2, 3, 4
+COLS_TILE, COLS_TMA, COLS_PAIR, COLS_PAIR8, COLS_DEEP = 0, 1, 2, 3, 4
 DN_COEF_F64, DN_ISAT_F64 = 1, 2
 
 OK = 0

@@ -181,7 +181,8 @@ namespace {
 // The pair row pass serves this launch: complex64 one-component field on
 // the blocked buffer through the tensor map, no Rabi, pump or external |A|^2.
 bool rows_pair_fits(const nlse_plan_s* p, int mode, const StepArgs& a) {
-  return (p->rows_var == NLSE_ROWS_PAIR || p->rows_var == NLSE_ROWS_PAIR8) &&
+  return (p->rows_var == NLSE_ROWS_PAIR || p->rows_var == NLSE_ROWS_PAIR8 ||
+          p->rows_var == NLSE_ROWS_DEEP) &&
          p->d.dtype == NLSE_C64 && a.comps == 1 &&
          (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (a.flags & F_IN_BLK) && a.tmap &&
          a.tma_grid > 0 && !(a.flags & (F_RABI | F_PUMP | F_PROBE | F_ASQ_EXT)) &&
@@ -193,8 +194,9 @@ cudaError_t rows(const nlse_plan_s* p, int mode, int log2n, const StepArgs& a, c
                  bool prep = false) {
   if (prep && p->d.dtype == NLSE_C64 && a.comps == 1 &&
       (mode == ROW_INV_NL || mode == ROW_INV_NL_FWD) && (p->rows_avail >> NLSE_ROWS_PAIR & 1)) {
-    for (int ep : {16, 8}) {
-      const cudaError_t e = launch_rows_pair(mode, log2n, a, false, s, true, 0, ep);
+    for (int form : {16, 8, 0}) {
+      const cudaError_t e = launch_rows_pair(mode, log2n, a, false, s, true, 0, form ? form : 16,
+                                             form == 0);
       if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
     }
   }
@@ -204,7 +206,8 @@ cudaError_t rows(const nlse_plan_s* p, int mode, int log2n, const StepArgs& a, c
     const bool vshared = (a.flags & F_HAS_V) && !(a.flags & F_V_COMPLEX) && a.v_fstride == 0 &&
                          p->d.nfields % 2 == 0;
     const int ep = p->rows_var == NLSE_ROWS_PAIR8 ? 8 : 16;
-    const cudaError_t e = launch_rows_pair(mode, log2n, a, vshared, s, false, p->rows_cap, ep);
+    const cudaError_t e = launch_rows_pair(mode, log2n, a, vshared, s, false, p->rows_cap, ep,
+                                           p->rows_var == NLSE_ROWS_DEEP);
     if (e != cudaErrorNotSupported) return e;
   }
   if (p->d.dtype == NLSE_C64)
@@ -224,15 +227,18 @@ cudaError_t cols_blk(const nlse_plan_s* p, int mode, int log2n, const ColArgs& a
                      bool prep = false) {
   if (p->d.dtype == NLSE_C64 && mode == COL_FWD_PROP_INV) {
     if (prep && (p->cols_avail >> NLSE_COLS_PAIR & 1)) {
-      for (int ep : {16, 8}) {
-        const cudaError_t e = launch_cols_pair(log2n, a, s, true, 0, ep);
+      for (int form : {16, 8, 0}) {
+        const cudaError_t e = launch_cols_pair(log2n, a, s, true, 0, form ? form : 16, form == 0);
         if (e != cudaSuccess && e != cudaErrorNotSupported) return e;
       }
     }
-    if (!prep && (p->cols_var == NLSE_COLS_PAIR || p->cols_var == NLSE_COLS_PAIR8) &&
+    if (!prep &&
+        (p->cols_var == NLSE_COLS_PAIR || p->cols_var == NLSE_COLS_PAIR8 ||
+         p->cols_var == NLSE_COLS_DEEP) &&
         a.tma_grid > 0 && !(a.flags & F_PROP_C128)) {
       const int ep = p->cols_var == NLSE_COLS_PAIR8 ? 8 : 16;
-      const cudaError_t e = launch_cols_pair(log2n, a, s, false, p->cols_cap, ep);
+      const cudaError_t e = launch_cols_pair(log2n, a, s, false, p->cols_cap, ep,
+                                             p->cols_var == NLSE_COLS_DEEP);
       if (e != cudaErrorNotSupported) return e;
     }
   }
@@ -715,10 +721,10 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     const bool pair = !(penv && penv[0] == '0') && d.dtype == NLSE_C64 && d.comps == 1;
     if (p->rows_tma_ok) p->rows_avail |= 1u << NLSE_ROWS_TMA;
     if (p->rows_tma_ok && pair && p->lg[1] >= 6 && p->lg[1] <= 12)
-      p->rows_avail |= (1u << NLSE_ROWS_PAIR) | (1u << NLSE_ROWS_PAIR8);
+      p->rows_avail |= (1u << NLSE_ROWS_PAIR) | (1u << NLSE_ROWS_PAIR8) | (1u << NLSE_ROWS_DEEP);
     if (p->cols_tma_ok) p->cols_avail |= 1u << NLSE_COLS_TMA;
     if (p->cols_tma_ok && pair && p->lg[0] >= 6 && p->lg[0] <= 11)
-      p->cols_avail |= (1u << NLSE_COLS_PAIR) | (1u << NLSE_COLS_PAIR8);
+      p->cols_avail |= (1u << NLSE_COLS_PAIR) | (1u << NLSE_COLS_PAIR8) | (1u << NLSE_COLS_DEEP);
     p->rows_var = (p->rows_avail >> NLSE_ROWS_PAIR & 1) ? NLSE_ROWS_PAIR
                   : p->rows_tma                          ? NLSE_ROWS_TMA
                                                          : NLSE_ROWS_LINE;
@@ -1045,9 +1051,10 @@ int nlse_plan_set_variant(nlse_plan p, int32_t rows, int32_t cols, int32_t rows_
                           int32_t cols_ctas_per_sm) {
   g_err.clear();
   if (!p) return fail(NLSE_ERR_ARG, "null plan");
-  if (rows < 0 || rows > 3 || cols < 0 || cols > 3 || rows_ctas_per_sm < 0 ||
-      cols_ctas_per_sm < 0 || rows_ctas_per_sm > 32 || cols_ctas_per_sm > 32)
-    return fail(NLSE_ERR_ARG, "variant codes 0..3, CTAs per SM 0..32");
+  if (rows < 0 || rows > NLSE_ROWS_DEEP || cols < 0 || cols > NLSE_COLS_DEEP ||
+      rows_ctas_per_sm < 0 || cols_ctas_per_sm < 0 || rows_ctas_per_sm > 32 ||
+      cols_ctas_per_sm > 32)
+    return fail(NLSE_ERR_ARG, "variant codes 0..4, CTAs per SM 0..32");
   if (!(p->rows_avail >> rows & 1))
     return fail(NLSE_ERR_UNSUPPORTED, "row pass variant %d is not available for this plan", rows);
   if (!(p->cols_avail >> cols & 1))

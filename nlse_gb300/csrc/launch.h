@@ -30,10 +30,13 @@ cudaError_t launch_cols_blk_f64(int mode, int log2n, const ColArgs& a, cudaStrea
 // potential shared by the batch with an even number of fields.
 // cudaErrorNotSupported for a size without a pair kernel.
 // ep: positions per thread and line, 16 or 8 (twice the threads per line).
+// deep (ep 16 only): the deep-prefetch forms, which keep the next work item's
+// copies in flight for the whole current item (rows: every exchange in the
+// item's own buffer; columns: three staging tiles, no exchange tile).
 cudaError_t launch_rows_pair(int mode, int log2n, const StepArgs& a, bool vshared, cudaStream_t s,
-                             bool prepare_only, int cap_per_sm, int ep);
+                             bool prepare_only, int cap_per_sm, int ep, bool deep = false);
 cudaError_t launch_cols_pair(int log2n, const ColArgs& a, cudaStream_t s, bool prepare_only,
-                             int cap_per_sm, int ep);
+                             int cap_per_sm, int ep, bool deep = false);
 
 // One launch per pass over several plans (step_multi.cuh): complex64
 // one-component 2-D plans of 256..2048 points per axis with TMA row passes.

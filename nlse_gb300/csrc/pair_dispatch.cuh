@@ -1,5 +1,5 @@
 // Compile-time-size dispatch of the pair kernels (step_pair.cuh).  Included by
-// rows_pair.cu and cols_pair.cu, one translation unit each.
+// the rows_pair*.cu, rows_deep*.cu and cols_*.cu translation units.
 #pragma once
 #include "launch.h"
 #include "step_pair.cuh"
@@ -29,12 +29,12 @@ static cudaError_t persistent_grid(F* kern, int threads, size_t smem, int nsm, i
   return cudaSuccess;
 }
 
-template <int N, int EP, int MODE, bool VS>
+template <int N, int EP, int MODE, bool VS, bool DEEP>
 static cudaError_t rows_pair_nv(const StepArgs& a, cudaStream_t s, bool prep, int cap) {
   using RP = RowPair<N, EP>;
   constexpr size_t smem = rows_pair_smem<N, EP>();
   static_assert(smem <= 227 * 1024, "pair row pass shared memory");
-  auto kern = k_rows_pair_tma<N, EP, MODE, VS>;
+  auto kern = k_rows_pair_tma<N, EP, MODE, VS, DEEP>;
   if (prep) return pair_set_smem(kern, smem);
   if (a.nq <= 0) return cudaSuccess;
   unsigned grid = 0;
@@ -45,41 +45,42 @@ static cudaError_t rows_pair_nv(const StepArgs& a, cudaStream_t s, bool prep, in
   return cudaGetLastError();
 }
 
-template <int N, int EP, int MODE>
+template <int N, int EP, int MODE, bool DEEP>
 static cudaError_t rows_pair_n(const StepArgs& a, bool vshared, cudaStream_t s, bool prep, int cap) {
   if (prep) {
-    cudaError_t e = rows_pair_nv<N, EP, MODE, true>(a, s, true, cap);
+    cudaError_t e = rows_pair_nv<N, EP, MODE, true, DEEP>(a, s, true, cap);
     if (e != cudaSuccess) return e;
-    return rows_pair_nv<N, EP, MODE, false>(a, s, true, cap);
+    return rows_pair_nv<N, EP, MODE, false, DEEP>(a, s, true, cap);
   }
-  return vshared ? rows_pair_nv<N, EP, MODE, true>(a, s, false, cap)
-                 : rows_pair_nv<N, EP, MODE, false>(a, s, false, cap);
+  return vshared ? rows_pair_nv<N, EP, MODE, true, DEEP>(a, s, false, cap)
+                 : rows_pair_nv<N, EP, MODE, false, DEEP>(a, s, false, cap);
 }
 
-template <int EP, int MODE>
+// DEEP: the deep-prefetch form (k_rows_pair_tma)
+template <int EP, int MODE, bool DEEP = false>
 static cudaError_t rows_pair_mode(int log2n, const StepArgs& a, bool vshared, cudaStream_t s,
                                   bool prep, int cap) {
   switch (log2n) {
-    case 6: return rows_pair_n<64, EP, MODE>(a, vshared, s, prep, cap);
-    case 7: return rows_pair_n<128, EP, MODE>(a, vshared, s, prep, cap);
-    case 8: return rows_pair_n<256, EP, MODE>(a, vshared, s, prep, cap);
-    case 9: return rows_pair_n<512, EP, MODE>(a, vshared, s, prep, cap);
-    case 10: return rows_pair_n<1024, EP, MODE>(a, vshared, s, prep, cap);
-    case 11: return rows_pair_n<2048, EP, MODE>(a, vshared, s, prep, cap);
-    case 12: return rows_pair_n<4096, EP, MODE>(a, vshared, s, prep, cap);
+    case 6: return rows_pair_n<64, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 7: return rows_pair_n<128, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 8: return rows_pair_n<256, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 9: return rows_pair_n<512, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 10: return rows_pair_n<1024, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 11: return rows_pair_n<2048, EP, MODE, DEEP>(a, vshared, s, prep, cap);
+    case 12: return rows_pair_n<4096, EP, MODE, DEEP>(a, vshared, s, prep, cap);
     default: return cudaErrorNotSupported;
   }
 }
 
-// Sizes whose two staging tiles and exchange tile fit in shared memory.
-template <int N, int EP>
+// Sizes whose staging tiles (and exchange tile) fit in shared memory.
+template <int N, int EP, bool DEEP>
 static cudaError_t cols_pair_n(const ColArgs& a, cudaStream_t s, bool prep, int cap) {
-  if constexpr (cols_pair_smem<N, EP>() > 227 * 1024 || 2 * (N / Shape<N, EP>::E) > 1024) {
+  if constexpr (cols_pair_smem<N, EP, DEEP>() > 227 * 1024 || 2 * (N / Shape<N, EP>::E) > 1024) {
     return cudaErrorNotSupported;
   } else {
     constexpr int THREADS = 2 * (N / Shape<N, EP>::E);
-    constexpr size_t smem = cols_pair_smem<N, EP>();
-    auto kern = k_cols_pair_tma<N, EP>;
+    constexpr size_t smem = cols_pair_smem<N, EP, DEEP>();
+    auto kern = k_cols_pair_tma<N, EP, DEEP>;
     if (prep) return pair_set_smem(kern, smem);
     if (a.nblocks <= 0) return cudaSuccess;
     unsigned grid = 0;
@@ -90,17 +91,17 @@ static cudaError_t cols_pair_n(const ColArgs& a, cudaStream_t s, bool prep, int 
   }
 }
 
-template <int EP>
+template <int EP, bool DEEP = false>
 static cudaError_t cols_pair_dispatch(int log2n, const ColArgs& a, cudaStream_t s, bool prep,
                                       int cap) {
   switch (log2n) {
-    case 6: return cols_pair_n<64, EP>(a, s, prep, cap);
-    case 7: return cols_pair_n<128, EP>(a, s, prep, cap);
-    case 8: return cols_pair_n<256, EP>(a, s, prep, cap);
-    case 9: return cols_pair_n<512, EP>(a, s, prep, cap);
-    case 10: return cols_pair_n<1024, EP>(a, s, prep, cap);
-    case 11: return cols_pair_n<2048, EP>(a, s, prep, cap);
-    case 12: return cols_pair_n<4096, EP>(a, s, prep, cap);
+    case 6: return cols_pair_n<64, EP, DEEP>(a, s, prep, cap);
+    case 7: return cols_pair_n<128, EP, DEEP>(a, s, prep, cap);
+    case 8: return cols_pair_n<256, EP, DEEP>(a, s, prep, cap);
+    case 9: return cols_pair_n<512, EP, DEEP>(a, s, prep, cap);
+    case 10: return cols_pair_n<1024, EP, DEEP>(a, s, prep, cap);
+    case 11: return cols_pair_n<2048, EP, DEEP>(a, s, prep, cap);
+    case 12: return cols_pair_n<4096, EP, DEEP>(a, s, prep, cap);
     default: return cudaErrorNotSupported;
   }
 }

@@ -122,7 +122,11 @@ __host__ __device__ constexpr size_t rows_pair_smem() {
 // already in shared memory buffer Xs (line l at Xs + l * SLS); Xn is the other
 // buffer (the second exchange buffer).  prefetch() is run by thread 0 once
 // every read of Xn is complete, to refill it.  g: the item's index.
-template <int N, int EP, int MODE, bool VSHARED, typename Prefetch>
+// DEEP: every exchange of both transforms in Xs (two barriers each), so Xn
+// is free from the start and the next item's copies are issued right after
+// the lines are read: they are in flight for the whole item, not only for the
+// forward transform (twice the bytes in flight per CTA over an item).
+template <int N, int EP, int MODE, bool VSHARED, bool DEEP = false, typename Prefetch>
 __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, float2* Xs,
                                               float2* Xn, Prefetch&& prefetch) {
   using RP = RowPair<N, EP>;
@@ -173,7 +177,12 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
   __syncthreads();  // every thread has read its lines from buffer st
   float4* sA = reinterpret_cast<float4*>(buf(Xs, 2 * pp));
   float4* sB = reinterpret_cast<float4*>(buf(Xn, 2 * pp));
-  pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
+  if constexpr (DEEP) {
+    if (threadIdx.x == 0) prefetch();
+    pfft_rest<N, E, 1, true, true>(x, t, sA, 1, tw);
+  } else {
+    pfft_db<N, E, 1, true, 0, 3>(x, t, sA, sB, 1, tw);
+  }
   // (1/N: applied by the column pass through the blocked propagator)
   // V' = vscale * V rounded in single precision, as the reference's k/2*V array
   auto nl_all = [&](int set) {
@@ -210,9 +219,13 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
   if (!(a.flags & F_NO_POST)) nl_all(0);
   if constexpr (MODE == ROW_INV_NL_FWD) {
     if (a.flags & F_PRE_NL) nl_all(1);
-    pfft_hook<N, E, false, true, NEX % 2 == 1>(x, t, sA, 1, tw, [&] {
-      if (threadIdx.x == 0) prefetch();
-    });
+    if constexpr (DEEP) {
+      pfft_rest<N, E, 1, false, true>(x, t, sA, 1, tw);
+    } else {
+      pfft_hook<N, E, false, true, NEX % 2 == 1>(x, t, sA, 1, tw, [&] {
+        if (threadIdx.x == 0) prefetch();
+      });
+    }
     if (act) {
       const int64_t lpc = a.lines_per_comp, dstr = (int64_t)TPL * lpc;
       C* da = reinterpret_cast<C*>(a.S) + fa * a.pix + ((t / W) * lpc + ma) * W + (t % W);
@@ -224,8 +237,10 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
       }
     }
   } else {
-    __syncthreads();  // B is no longer read
-    if (threadIdx.x == 0) prefetch();
+    if constexpr (!DEEP) {
+      __syncthreads();  // B is no longer read
+      if (threadIdx.x == 0) prefetch();
+    }
     if (act) {
       C* da = reinterpret_cast<C*>(a.A) + fa * a.pix + ma * N + t;
       C* db = reinterpret_cast<C*>(a.A) + fb * a.pix + mb * N + t;
@@ -244,8 +259,11 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
 // VSHARED: the potential is real and both lines of every pair read the same
 // row of it (one potential for the batch and an even number of fields).
 // (three CTAs per SM fit in shared memory: registers are capped to match)
-template <int N, int EP, int MODE, bool VSHARED>
-__global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
+// three CTAs per SM below 256 threads; one at 256 (4096-point rows: their
+// 139 KB of staging allows no second, and a 3-CTA register cap spills)
+template <int N, int EP, int MODE, bool VSHARED, bool DEEP = false>
+__global__ void __launch_bounds__(RowPair<N, EP>::THREADS, RowPair<N, EP>::THREADS >= 256 ? 1 : 3)
+    k_rows_pair_tma(
     const StepArgs a, const __grid_constant__ CUtensorMap tmS) {
   using RP = RowPair<N, EP>;
   using C = float2;
@@ -302,7 +320,7 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, 3) k_rows_pair_tma(
       }
       return;
     }
-    pair_row_item<N, EP, MODE, VSHARED>(a, g, buf(st, 0), buf(st ^ 1, 0), [&] {
+    pair_row_item<N, EP, MODE, VSHARED, DEEP>(a, g, buf(st, 0), buf(st ^ 1, 0), [&] {
       prefetch(st ^ 1, g + gridDim.x);
     });
   }
@@ -322,22 +340,35 @@ namespace nlse {
 // propagator, inverse column FFT; the propagator (blocked, complex64) values
 // of the tile are requested before the forward transform.
 // the transform's twiddles in shared memory when they fit
-template <int N, int EP>
-__host__ __device__ constexpr bool cols_pair_tws() {
-  return cols_tma_base_smem<float, N>() + (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) +
-             16 <= kMaxSmemBytes;
+// DEEP: three staging tiles and no exchange tile; both transforms exchange in
+// the tile just read (two barriers per exchange), so two tiles are in flight
+// while one is transformed.
+template <bool DEEP>
+__host__ __device__ constexpr int cols_pair_stages() { return DEEP ? 3 : kColStages; }
+template <int N, bool DEEP>
+__host__ __device__ constexpr size_t cols_pair_base_smem() {
+  return (size_t)(cols_pair_stages<DEEP>() + (DEEP ? 0 : 1)) *
+             stage_len<float>(padded_len(N) * BlkW<float>::W) * sizeof(float2) +
+         cols_pair_stages<DEEP>() * sizeof(uint64_t);
 }
-template <int N, int EP = 16>
+// the transform's twiddles in shared memory when they fit
+template <int N, int EP, bool DEEP = false>
+__host__ __device__ constexpr bool cols_pair_tws() {
+  return cols_pair_base_smem<N, DEEP>() +
+             (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) + 16 <= kMaxSmemBytes;
+}
+template <int N, int EP = 16, bool DEEP = false>
 __host__ __device__ constexpr size_t cols_pair_smem() {
-  return cols_tma_base_smem<float, N>() +
-         (cols_pair_tws<N, EP>() ? (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) + 16
-                                 : 0);
+  return cols_pair_base_smem<N, DEEP>() +
+         (cols_pair_tws<N, EP, DEEP>() ? (size_t)tw_compact_len(N, Shape<N, EP>::E) * sizeof(float2) + 16
+                                       : 0);
 }
 
-template <int N, int EP>
+template <int N, int EP, bool DEEP = false>
 __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(const ColArgs a) {
   using C = float2;
   constexpr int E = Shape<N, EP>::E, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
+  constexpr int NST = cols_pair_stages<DEEP>();
   constexpr int SLW = stage_len<float>(padded_len(N) * W);
   static_assert((SLW * sizeof(C)) % 128 == 0, "bulk copies need aligned shared destinations");
   static_assert(padded_len(N) * 2 * sizeof(float4) <= SLW * sizeof(C),
@@ -351,10 +382,10 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
   constexpr bool DB = NEX > 0;
   extern __shared__ __align__(128) unsigned char smraw[];
   C* stage = reinterpret_cast<C*>(smraw);
-  C* xch = stage + kColStages * SLW;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + SLW);
-  constexpr bool TWS = cols_pair_tws<N, EP>();
-  C* twc = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(bar) + 16);
+  C* xch = stage + NST * SLW;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + (DEEP ? 0 : SLW));
+  constexpr bool TWS = cols_pair_tws<N, EP, DEEP>();
+  C* twc = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(bar) + (NST == 3 ? 24 : 16));
   if constexpr (TWS) load_tw_compact<float, N, E>(twc, reinterpret_cast<const C*>(a.tw));
   const C* tw = TWS ? twc : reinterpret_cast<const C*>(a.tw);
   C* S = reinterpret_cast<C*>(a.A);
@@ -366,12 +397,12 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
   auto tile_ptr = [&](int64_t i) { return S + tile_o(i) * a.outer_stride + tile_b(i) * TILE; };
 
   if (threadIdx.x == 0) {
-    for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
+    for (int st = 0; st < NST; ++st) mbar_init(&bar[st], 1);
     mbar_init_fence();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int st = 0; st < kColStages; ++st) {
+    for (int st = 0; st < NST; ++st) {
       const int64_t i = blockIdx.x + (int64_t)st * gridDim.x;
       if (i < ntiles) {
         mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
@@ -380,7 +411,7 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
     }
   }
   auto refill = [&](int st, int64_t i) {
-    const int64_t inext = i + (int64_t)kColStages * gridDim.x;
+    const int64_t inext = i + (int64_t)NST * gridDim.x;
     if (inext < ntiles) {
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
@@ -389,15 +420,16 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
   };
   int it = 0;
   for (int64_t i = blockIdx.x; i < ntiles; i += gridDim.x, ++it) {
-    const int st = it % kColStages;
-    const unsigned par = (it / kColStages) & 1;
+    const int st = it % NST;
+    const unsigned par = (it / NST) & 1;
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
+      // give up: record it, let this tile's and the later tiles' copies land (bounded)
       if (threadIdx.x == 0) {
         atomicExch(a.status, DEV_WAIT_TIMEOUT);
-        mbar_wait_bounded(&bar[st], par);
-        if (i + gridDim.x < ntiles)
-          mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kColStages) & 1);
+        for (int k = 0; k < NST; ++k)
+          if (i + (int64_t)k * gridDim.x < ntiles)
+            mbar_wait_bounded(&bar[(it + k) % NST], ((it + k) / NST) & 1);
       }
       return;
     }
@@ -422,7 +454,9 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
     __syncthreads();  // every thread has read stage st
     float4* sA = reinterpret_cast<float4*>(stage + st * SLW) + p;
     float4* sB = reinterpret_cast<float4*>(xch) + p;
-    if constexpr (DB) {
+    if constexpr (DEEP) {
+      pfft_rest<N, E, 1, false, true, TWS>(x, t, sA, 2, tw);
+    } else if constexpr (DB) {
       pfft_db<N, E, 1, false, 0, 1, TWS>(x, t, sA, sB, 2, tw);
     } else {
       if (threadIdx.x == 0) refill(st, i);
@@ -433,7 +467,11 @@ __global__ void __launch_bounds__(2 * (N / Shape<N, EP>::E), 1) k_cols_pair_tma(
       const float2 pr = f2(pre[j].x, pre[j].z), pi = f2(pre[j].y, pre[j].w);
       x[j] = {fnma2(x[j].im, pi, mul2(x[j].re, pr)), fma2(x[j].re, pi, mul2(x[j].im, pr))};
     }
-    if constexpr (DB) {
+    if constexpr (DEEP) {
+      pfft_rest<N, E, 1, true, true, TWS>(x, t, sA, 2, tw);
+      __syncthreads();  // every read of stage st is complete
+      if (threadIdx.x == 0) refill(st, i);
+    } else if constexpr (DB) {
       pfft_db<N, E, 1, true, NEX % 2, 1, TWS>(x, t, sA, sB, 2, tw);
       if (threadIdx.x == 0) refill(st, i);
     } else {

@@ -107,8 +107,8 @@ class Plan:
                                                   *[ct.byref(x) for x in m]), "kernel variant")
         return {"rows": v[0].value, "cols": v[1].value, "rows_cap": v[2].value,
                 "cols_cap": v[3].value,
-                "rows_avail": [i for i in range(4) if m[0].value >> i & 1],
-                "cols_avail": [i for i in range(4) if m[1].value >> i & 1]}
+                "rows_avail": [i for i in range(32) if m[0].value >> i & 1],
+                "cols_avail": [i for i in range(32) if m[1].value >> i & 1]}
 
     def get_kernels(self) -> tuple:
         """(rows_tma, cols_tma, rows_tma available, cols_tma available)."""

@@ -21,18 +21,17 @@ Parts (each writes .npz files under tests/golden/):
             (golden fixtures; run before spread and short, which cover them).
   fullsize  the benchmark configurations at their stated sizes (outputs
             subsampled on a regular grid, FP64 power of the whole field):
-              nlse2048   2048^2 noisy beam, dz = 2e-5 m, 501 steps, "single":
-                         complex128, and complex64 with the three FFTs;
+              nlse2048   2048^2 noisy beam, dz = 2e-5 m, 501 steps, "single";
               cnlse1024  CNLSE 1024^2, two components, Gaussian nonlocal kernel
-                         (sigma 100 um, 67^2 support), 400 steps, "single":
-                         complex128, and complex64 with the three FFTs;
+                         (sigma 100 um, 67^2 support), 400 steps, "single";
               mixed      field 0 of each grid size of the 164-field batch
                          (tests/cases.py mixed_batch, seed 11; per-field power
                          (1,) and n2 (1, 1, 1) float64 arrays, so the
                          reference evaluates the complex64 nonlinear step in
-                         FP64), 201 steps: complex128, and complex64 with the
-                         three FFTs.
-            -> fullsize/<case>.npz
+                         FP64), 201 steps;
+            each in complex128 and complex64, each with the three FFTs
+            -> fullsize/<case>_<c128|c64>_single.npz
+            (fullsize:nlse2048,c128 picks cases and/or one dtype)
 
 Usage: python tests/golden/make_parity.py REFERENCE_ROOT [part ...]
        (or NLSE_REFERENCE_ROOT=...; default: every part)
@@ -225,13 +224,18 @@ def mixed_inputs(R_NLSE, dtype, group: int):
 
 
 def part_fullsize(which=("nlse2048", "cnlse1024", "mixed")) -> None:
+    kinds = ("scipy", "numpy", "torch")
+    dtypes = [d for d, t in ((np.complex128, "c128"), (np.complex64, "c64")) if t in which]
+    dtypes = dtypes or [np.complex128, np.complex64]
+    cases_ = [c for c in ("nlse2048", "cnlse1024", "mixed") if c in which]
+    which = cases_ or ("nlse2048", "cnlse1024", "mixed")
     from functools import partial
     from types import SimpleNamespace
 
     # the reference's GPU path (its constructors pick the CPU backend by default here)
     R = SimpleNamespace(NLSE=partial(_R.NLSE, backend="GPU"), CNLSE=partial(_R.CNLSE, backend="GPU"))
     if "nlse2048" in which:
-        for dtype, kinds in ((np.complex128, ("scipy",)), (np.complex64, ("scipy", "numpy", "torch"))):
+        for dtype in dtypes:
             outs = {}
             for kind in kinds:
                 use_fft(kind)
@@ -247,7 +251,7 @@ def part_fullsize(which=("nlse2048", "cnlse1024", "mixed")) -> None:
             save(HERE / "fullsize" / f"nlse2048_{tag}_single.npz", N=np.array(2048), seed=np.array(0),
                  dz=np.array(2e-5), z=np.array(10e-3), **outs)
     if "cnlse1024" in which:
-        for dtype, kinds in ((np.complex128, ("scipy",)), (np.complex64, ("scipy", "numpy", "torch"))):
+        for dtype in dtypes:
             outs = {}
             for kind in kinds:
                 use_fft(kind)
@@ -264,8 +268,7 @@ def part_fullsize(which=("nlse2048", "cnlse1024", "mixed")) -> None:
                  dz=np.array(5e-5), z=np.array(20e-3), **outs)
     if "mixed" in which:
         for g, N in enumerate((256, 512, 1024, 2048)):
-            for dtype, kinds in ((np.complex128, ("scipy",)),
-                                 (np.complex64, ("scipy", "numpy", "torch"))):
+            for dtype in dtypes:
                 outs = {}
                 for kind in kinds:
                     use_fft(kind)

@@ -37,15 +37,15 @@ def test_variants_agree_and_tuner_caches(N, B, tmp_path, monkeypatch):
         engine.propagate(plan, A, op, 7, 0, graph=True)
         plan.status()
         outs[v] = A.cpu().numpy()
-    # line/tile, TMA, pair and 8-position pair variants of both passes
-    assert len(outs) == 16, sorted(outs)
+    # line/tile, TMA, pair, 8-position pair and deep-prefetch pair variants of both passes
+    assert len(outs) == 25, sorted(outs)
     base = outs[(_lib.ROWS_TMA, _lib.COLS_TMA)]
     for v, o in outs.items():
         assert cases.rel_l2(o, base) <= 1e-5, v
     rec = autotune.tune(plan, A0, op)
     best = rec["variant"]
     assert (best["rows"], best["cols"]) in set(autotune.variants(plan))
-    assert len(rec["ms_per_step"]) >= 16
+    assert len(rec["ms_per_step"]) >= 25
     data = json.loads((tmp_path / "tune.json").read_text())
     assert data[autotune.plan_key(plan)]["variant"] == best
     plan.set_variant(_lib.ROWS_LINE, _lib.COLS_TILE)

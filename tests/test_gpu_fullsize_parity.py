@@ -10,11 +10,15 @@ the whole field:
              power are per-field float64 arrays, so the reference evaluates
              the complex64 nonlinear step in FP64 while the product keeps
              FP32.
-complex128: rel-L2 <= 1e-12 on the subsample and the power.  complex64:
-rel-L2 against the reference's complex64 result within max(1e-5,
-2 x the reference's own FFT spread) -- the reference itself moves that much
-when only its FFT changes -- and the error against the complex128 run
-within 2x the reference's own (or 1e-5).
+Both dtypes are held to the reference's own FFT spread: the fixtures hold the
+reference run three times, with scipy's, NumPy's and torch's FFT, and the
+product must agree with the scipy run within 2 x the larger of the other two
+runs' distances from it (floors: 1e-12 for complex128, 1e-5 for complex64).
+The noisy 2048^2 beam is modulationally unstable, so FP64 rounding grows over
+its 501 steps (the reference's complex128 runs differ by ~1e-8 from FFT
+rounding alone); a fixed 1e-12 would test the FFT library, not the path.
+complex64 also keeps its error against the complex128 run within 2x the
+reference's own (or 1e-5).
 """
 
 from pathlib import Path
@@ -42,19 +46,32 @@ def _fixture(name):
         return {k: z[k] for k in z.files}
 
 
+def _spread(f):
+    """How far the reference moves when only its FFT changes (field, power)."""
+    ref, pref = f["sub_scipy"], f["power_scipy"]
+    if "sub_numpy" not in f:
+        return 0.0, 0.0
+    field = max(cases.rel_l2(f["sub_numpy"], ref), cases.rel_l2(f["sub_torch"], ref))
+    power = max(float(np.max(np.abs(f[k] / pref - 1))) for k in ("power_numpy", "power_torch"))
+    return field, power
+
+
 def _check_c128(tag, got, f):
     sub = cases.subsample(got)
     err = cases.rel_l2(sub, f["sub_scipy"])
     perr = float(np.max(np.abs(cases.power_fp64(got) / f["power_scipy"] - 1)))
-    print(f"{tag} complex128: rel-L2 vs reference {err:.2e}, power {perr:.2e}")
-    assert err <= C128_TOL and perr <= C128_TOL, (err, perr)
+    spread, pspread = _spread(f)
+    print(f"{tag} complex128: rel-L2 vs reference {err:.2e} (reference FFT spread "
+          f"{spread:.2e}), power {perr:.2e} (spread {pspread:.2e})")
+    assert err <= max(SPREAD_SLACK * spread, C128_TOL), (err, spread)
+    assert perr <= max(SPREAD_SLACK * pspread, C128_TOL), (perr, pspread)
 
 
 def _check_c64(tag, got, f, f128):
     sub = cases.subsample(got)
     ref = f["sub_scipy"]
     err = cases.rel_l2(sub, ref)
-    spread = max(cases.rel_l2(f["sub_numpy"], ref), cases.rel_l2(f["sub_torch"], ref))
+    spread = _spread(f)[0]
     truth = f128["sub_scipy"]
     e64, e64_ref = cases.rel_l2(sub, truth), cases.rel_l2(ref, truth)
     print(f"{tag} complex64: vs reference {err:.2e} (reference FFT spread {spread:.2e}); vs "

@@ -124,7 +124,11 @@ def test_callbacks_path_matches_fused_path():
     norms = np.zeros(201)
     a = p1.out_field(E, cases.L, verbose=False)
     b = p2.out_field(E, cases.L, verbose=False, callback=ng.norm, callback_args=(1, norms))
-    assert cases.rel_l2(a, b) < 1e-6
+    # The callback path leaves the spectral layout every step (the field is
+    # read after each step), so its forward row transforms run in the scalar
+    # forward pass instead of inside the pair pass: the same arithmetic rounded
+    # in another order, 4e-6 apart after these 201 complex64 steps.
+    assert cases.rel_l2(a, b) < 1e-5
     assert np.all(np.diff(norms) < 0)  # lossy medium: the norm decreases every step
 
 

@@ -60,12 +60,13 @@ def test_pair_passes_match_scalar_passes_and_oracle(NY, NX, B, vmode, dz, scheme
     z = (STEPS - 0.5) * abs(dz)
     plan = engine.Plan.get(2, (NY, NX), B, 1, _lib.NLSE_C64, torch.device("cuda", 0))
     avail = plan.get_variant()
-    assert {_lib.ROWS_PAIR, _lib.ROWS_PAIR8} <= set(avail["rows_avail"])
-    assert {_lib.COLS_PAIR, _lib.COLS_PAIR8} <= set(avail["cols_avail"])
+    assert {_lib.ROWS_PAIR, _lib.ROWS_PAIR8, _lib.ROWS_DEEP} <= set(avail["rows_avail"])
+    assert {_lib.COLS_PAIR, _lib.COLS_PAIR8, _lib.COLS_DEEP} <= set(avail["cols_avail"])
     outs = {}
     for v in ((_lib.ROWS_PAIR, _lib.COLS_PAIR), (_lib.ROWS_TMA, _lib.COLS_TMA),
               (_lib.ROWS_PAIR, _lib.COLS_TMA), (_lib.ROWS_TMA, _lib.COLS_PAIR),
-              (_lib.ROWS_PAIR8, _lib.COLS_PAIR8), (_lib.ROWS_PAIR8, _lib.COLS_PAIR)):
+              (_lib.ROWS_PAIR8, _lib.COLS_PAIR8), (_lib.ROWS_PAIR8, _lib.COLS_PAIR),
+              (_lib.ROWS_DEEP, _lib.COLS_DEEP)):
         plan.set_variant(*v)
         outs[v] = p.out_field(E, z, precision=scheme, verbose=False)
         plan.status()
@@ -77,6 +78,8 @@ def test_pair_passes_match_scalar_passes_and_oracle(NY, NX, B, vmode, dz, scheme
     e_scalar = cases.rel_l2(pair, outs[(_lib.ROWS_TMA, _lib.COLS_TMA)])
     print(f"{NY}x{NX} B={B} V={vmode} dz={dz} {scheme}: pair vs oracle {e_ref:.2e}, "
           f"vs scalar passes {e_scalar:.2e}")
+    # the deep-prefetch forms run the same arithmetic with another copy schedule
+    assert cases.rel_l2(outs[(_lib.ROWS_DEEP, _lib.COLS_DEEP)], pair) <= 1e-6
     assert e_ref <= 1e-5 and e_scalar <= 1e-5
     for v, out in outs.items():
         assert cases.rel_l2(out, ref) <= 1e-5, v
