@@ -120,6 +120,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-surrogate", action="store_true",
                     help="leave out the surrogate-vs-solver leg (about a minute)")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="only time the 164-field mixed batch (--steps steps per call; for "
+                         "profiling)")
     ap.add_argument("--network-only", type=int, default=0, metavar="FIELDS",
                     help="only time the surrogate network's inference on FIELDS random "
                          "256^2 inputs (--steps passes after one warm-up; for profiling)")
@@ -524,41 +527,7 @@ def run_gb300(args):
                  "note": "CNLSE 1024^2 complex64, two components, Gaussian nonlocal kernel "
                          "(linear convolution on a zero-padded 2048^2 grid every step), "
                          "400-step out_field loop from device memory, L2 flushed between loops"}
-    # the 164-field mixed batch (96 @ 256^2, 48 @ 512^2, 16 @ 1024^2, 4 @ 2048^2), one
-    # grouped graph launch for the whole loop; inputs resident on the device
-    from tests import cases
-
-    jobs = cases.mixed_batch([(96, 256), (48, 512), (16, 1024), (4, 2048)], seed=11 + rank)
-    jobs = [(sim, torch.from_numpy(E).to(dev)) for sim, E in jobs]
-    zb = (args.steps - 0.5) * 5e-5
-    nb = ng.count_steps(zb, 5e-5)
-    from nlse_gb300 import batch as ngb
-
-    ng.out_fields(jobs, zb)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    tbs = []
-    for _ in range(7):
-        a.record()
-        ng.out_fields(jobs, zb)
-        b.record()
-        torch.cuda.synchronize()
-        tbs.append(a.elapsed_time(b) / 1e3)
-    tb = float(np.median(tbs))
-    if dist:
-        tt = torch.tensor([tb], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tb = float(tt.item())
-    rates = sorted(world * 164 * nb / x for x in tbs)
-    mixed = {"fields": 164, "steps": nb, "field_steps_per_s": world * 164 * nb / tb,
-             "replays": len(tbs), "field_steps_per_s_min_max": [rates[0], rates[-1]],
-             "fused": ngb.last_fused, "launches_per_step": 2 if ngb.last_fused else None,
-             "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
-                     "and potentials, device-resident; out_fields (one CUDA graph: one column "
-                     "pass and one row pass per step over every grid size when fused); median "
-                     "of the replays"}
+    mixed = mixed_batch_leg(args.steps, dev, rank, world, dist)
     stand_in = None
     if rank == 0:
         stand_in = gpu_stand_in(dev, E_host, V, sim, plan, op)
@@ -589,6 +558,75 @@ def run_gb300(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+MIXED_GROUPS = [(96, 256), (48, 512), (16, 1024), (4, 2048)]
+
+
+def mixed_batch_leg(steps, dev, rank=0, world=1, dist=None):
+    """The 164-field mixed batch (96 @ 256^2, 48 @ 512^2, 16 @ 1024^2, 4 @ 2048^2)
+    through out_fields, inputs resident on the device: median of 7 calls of
+    `steps` steps, and the loop's own rate from calls of steps and 3 x steps
+    (the difference removes the per-call set-up)."""
+    import torch
+
+    import nlse_gb300 as ng
+    from nlse_gb300 import batch as ngb
+    from tests import cases
+
+    jobs = cases.mixed_batch(MIXED_GROUPS, seed=11 + rank)
+    jobs = [(sim, torch.from_numpy(E).to(dev)) for sim, E in jobs]
+    nf = sum(n for n, _ in MIXED_GROUPS)
+
+    def calls(nsteps, reps=7):
+        z = (nsteps - 0.5) * 5e-5
+        ng.out_fields(jobs, z)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        ts = []
+        for _ in range(reps):
+            a.record()
+            ng.out_fields(jobs, z)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        t = float(np.median(ts))
+        if dist:
+            tt = torch.tensor([t], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        return ng.count_steps(z, 5e-5), t, ts
+
+    nb, tb, tbs = calls(steps)
+    nb3, tb3, _ = calls(3 * steps)
+    loop = (tb3 - tb) / (nb3 - nb)
+    rates = sorted(world * nf * nb / x for x in tbs)
+    return {"fields": nf, "steps": nb, "field_steps_per_s": world * nf * nb / tb,
+            "replays": len(tbs), "field_steps_per_s_min_max": [rates[0], rates[-1]],
+            "loop_field_steps_per_s": world * nf / loop, "loop_ms_per_step": loop * 1e3,
+            "call_setup_ms": (tb - nb * loop) * 1e3,
+            "fused": ngb.last_fused, "launches_per_step": 2 if ngb.last_fused else None,
+            "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
+                    "and potentials, device-resident; out_fields (one CUDA graph: one column "
+                    "pass and one row pass per step over every grid size when fused); "
+                    "field_steps_per_s: median of 7 calls of `steps` steps including each "
+                    "call's set-up (uploads of parameters, normalisation, first forward "
+                    "pass); loop_*: per step, from the difference between calls of "
+                    f"{3 * steps} and {steps} steps"}
+
+
+def mixed_only(args):
+    """Only the mixed-batch leg (for profiling its kernels)."""
+    import torch
+
+    from nlse_gb300 import _build
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    print(json.dumps({"mixed_batch_164": mixed_batch_leg(args.steps, dev)}))
 
 
 def network_only(args):
@@ -623,6 +661,8 @@ def main():
     args = parse()
     if args.network_only:
         network_only(args)
+    elif args.mixed_only:
+        mixed_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

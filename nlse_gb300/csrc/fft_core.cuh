@@ -53,13 +53,45 @@ __device__ __forceinline__ cpx<T> mk(T x, T y) {
   r.y = y;
   return r;
 }
+// Packed FP32 (f32x2, sm_100+): one instruction on both halves of a 64-bit
+// register pair, each half rounded as the scalar instruction would round it.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(r)
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
+        "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return *reinterpret_cast<const float2*>(&r);
+}
+
+// Complex sums and differences; a complex64 value {re, im} is one register
+// pair, so these are single packed instructions (same results as two scalar
+// ones).
 template <typename T>
 __device__ __forceinline__ cpx<T> cadd(cpx<T> a, cpx<T> b) {
-  return mk<T>(a.x + b.x, a.y + b.y);
+  if constexpr (sizeof(T) == 4) return add2(a, b);
+  else return mk<T>(a.x + b.x, a.y + b.y);
 }
 template <typename T>
 __device__ __forceinline__ cpx<T> csub(cpx<T> a, cpx<T> b) {
-  return mk<T>(a.x - b.x, a.y - b.y);
+  if constexpr (sizeof(T) == 4) return sub2(a, b);
+  else return mk<T>(a.x - b.x, a.y - b.y);
+}
+// a + rot(b) and a - rot(b), rot = multiplication by -i (forward) or +i
+// (inverse), the rotation folded into scalar additions (a packed form would
+// first have to build the rotated pair).
+template <typename T, bool INV>
+__device__ __forceinline__ cpx<T> cadd_rot(cpx<T> a, cpx<T> b) {
+  return INV ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, a.y - b.x);
+}
+template <typename T, bool INV>
+__device__ __forceinline__ cpx<T> csub_rot(cpx<T> a, cpx<T> b) {
+  return INV ? mk<T>(a.x + b.y, a.y - b.x) : mk<T>(a.x - b.y, a.y + b.x);
 }
 template <typename T>
 __device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b) {
@@ -103,11 +135,21 @@ template <typename T, bool INV> struct DFT<T, 2, INV> {
 template <typename T, bool INV>
 __device__ __forceinline__ void dft4(cpx<T>& a0, cpx<T>& a1, cpx<T>& a2, cpx<T>& a3) {
   const cpx<T> t0 = cadd<T>(a0, a2), t1 = csub<T>(a0, a2);
-  const cpx<T> t2 = cadd<T>(a1, a3), t3 = mul_mi<T, INV>(csub<T>(a1, a3));
+  const cpx<T> t2 = cadd<T>(a1, a3), d = csub<T>(a1, a3);
   a0 = cadd<T>(t0, t2);
-  a1 = cadd<T>(t1, t3);
+  a1 = cadd_rot<T, INV>(t1, d);
   a2 = csub<T>(t0, t2);
-  a3 = csub<T>(t1, t3);
+  a3 = csub_rot<T, INV>(t1, d);
+}
+// dft4 of (a0, a1, rot(a2), a3): the rotation of the third input folded in.
+template <typename T, bool INV>
+__device__ __forceinline__ void dft4_rot2(cpx<T>& a0, cpx<T>& a1, cpx<T>& a2, cpx<T>& a3) {
+  const cpx<T> t0 = cadd_rot<T, INV>(a0, a2), t1 = csub_rot<T, INV>(a0, a2);
+  const cpx<T> t2 = cadd<T>(a1, a3), d = csub<T>(a1, a3);
+  a0 = cadd<T>(t0, t2);
+  a1 = cadd_rot<T, INV>(t1, d);
+  a2 = csub<T>(t0, t2);
+  a3 = csub_rot<T, INV>(t1, d);
 }
 
 template <typename T, bool INV> struct DFT<T, 4, INV> {
@@ -122,14 +164,13 @@ template <typename T, bool INV> struct DFT<T, 8, INV> {
     dft4<T, INV>(o0, o1, o2, o3);
     const T r = T(NLSE_R2);
     o1 = mul_w<T, INV>(o1, r, r);
-    o2 = mul_mi<T, INV>(o2);
     o3 = mul_w<T, INV>(o3, -r, r);
     x[0] = cadd<T>(e0, o0);
     x[4] = csub<T>(e0, o0);
     x[1] = cadd<T>(e1, o1);
     x[5] = csub<T>(e1, o1);
-    x[2] = cadd<T>(e2, o2);
-    x[6] = csub<T>(e2, o2);
+    x[2] = cadd_rot<T, INV>(e2, o2);
+    x[6] = csub_rot<T, INV>(e2, o2);
     x[3] = cadd<T>(e3, o3);
     x[7] = csub<T>(e3, o3);
   }
@@ -146,14 +187,15 @@ template <typename T, bool INV> struct DFT<T, 16, INV> {
     x[1 + 4 * 2] = mul_w<T, INV>(x[1 + 4 * 2], r2, r2);    // W^2
     x[1 + 4 * 3] = mul_w<T, INV>(x[1 + 4 * 3], s8, c8);    // W^3
     x[2 + 4 * 1] = mul_w<T, INV>(x[2 + 4 * 1], r2, r2);    // W^2
-    x[2 + 4 * 2] = mul_mi<T, INV>(x[2 + 4 * 2]);           // W^4
+    // x[2 + 4 * 2] times W^4 (the rotation), folded into its dft4 below
     x[2 + 4 * 3] = mul_w<T, INV>(x[2 + 4 * 3], -r2, r2);   // W^6
     x[3 + 4 * 1] = mul_w<T, INV>(x[3 + 4 * 1], s8, c8);    // W^3
     x[3 + 4 * 2] = mul_w<T, INV>(x[3 + 4 * 2], -r2, r2);   // W^6
     x[3 + 4 * 3] = mul_w<T, INV>(x[3 + 4 * 3], -c8, -s8);  // W^9
-#pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1)
-      dft4<T, INV>(x[4 * k1 + 0], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
+    dft4<T, INV>(x[0], x[1], x[2], x[3]);
+    dft4<T, INV>(x[4], x[5], x[6], x[7]);
+    dft4_rot2<T, INV>(x[8], x[9], x[10], x[11]);
+    dft4<T, INV>(x[12], x[13], x[14], x[15]);
     // x[4*k1 + k2] holds y[k1 + 4*k2]; transpose the 4x4 index in registers.
     cpx<T> y[16];
 #pragma unroll

@@ -27,19 +27,6 @@ struct __align__(16) cp2 {
   float2 re, im;
 };
 
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-  unsigned long long r;
-  asm("sub.rn.f32x2 %0, %1, %2;"
-      : "=l"(r)
-      : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
-        "l"(*reinterpret_cast<const unsigned long long*>(&b)));
-  return *reinterpret_cast<const float2*>(&r);
-}
 // c - a * b
 __device__ __forceinline__ float2 fnma2(float2 a, float2 b, float2 c) {
   return __ffma2_rn(a, make_float2(-b.x, -b.y), c);

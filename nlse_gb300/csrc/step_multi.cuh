@@ -108,6 +108,12 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
         tensor_load_4d(X + b * kMultiRowHalf + l * SLS + bx * BOXB * W, &m.tm[k], 0, (int)y,
                        bx * BOXB, (int)f, &bar[b]);
     }
+    switch (P.log2n) {
+      case 8: pair_prefetch_inputs<256, 16>(P.a, item - P.item0); break;
+      case 9: pair_prefetch_inputs<512, 16>(P.a, item - P.item0); break;
+      case 10: pair_prefetch_inputs<1024, 16>(P.a, item - P.item0); break;
+      default: pair_prefetch_inputs<2048, 16>(P.a, item - P.item0); break;
+    }
   };
   if (threadIdx.x == 0) {
     for (int st = 0; st < kRowStages; ++st) mbar_init(&bar[st], 1);

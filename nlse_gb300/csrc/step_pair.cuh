@@ -122,6 +122,39 @@ __host__ __device__ constexpr size_t rows_pair_smem() {
 // already in shared memory buffer Xs (line l at Xs + l * SLS); Xn is the other
 // buffer (the second exchange buffer).  prefetch() is run by thread 0 once
 // every read of Xn is complete, to refill it.  g: the item's index.
+// The per-line inputs the nonlinear step of work item g reads from global
+// memory -- a potential that differs between fields (v_fstride > 0) and the
+// coefficient planes -- prefetched into L2 when the item's lines are
+// requested (thread 0), so that those loads, issued after the inverse
+// transform, hit L2 instead of waiting on HBM.  A potential shared by the
+// fields stays in L2 by itself.
+template <int N, int EP>
+__device__ __forceinline__ void pair_prefetch_inputs(const StepArgs& a, unsigned g) {
+  constexpr int LPC = RowPair<N, EP>::LPC;
+  // (bulk prefetches need 16-byte aligned rows: a potential or planes at an
+  // odd offset are simply not prefetched)
+  const bool pv = (a.flags & F_HAS_V) && a.v_fstride != 0 &&
+                  (reinterpret_cast<uintptr_t>(a.V) & 15) == 0;
+  const bool pm = (a.flags & F_MAPS) && a.maps_mask &&
+                  (reinterpret_cast<uintptr_t>(a.maps) & 15) == 0;
+  if (!pv && !pm) return;
+  const unsigned nq = (unsigned)a.nq, nf = nq / (unsigned)a.lines_per_comp;
+  const unsigned q0 = g * LPC;
+  const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+  const unsigned vb = (a.flags & F_V_COMPLEX) ? 8u : 4u;
+  for (unsigned l = 0; l < nl; ++l) {
+    const int64_t f = (q0 + l) % nf, y = (q0 + l) / nf;
+    if (pv)
+      bulk_prefetch_l2(reinterpret_cast<const unsigned char*>(a.V) +
+                           (f * a.v_fstride + y * (int64_t)N) * vb, N * vb);
+    if (pm) {
+      const float* M = reinterpret_cast<const float*>(a.maps) + f * a.maps_fstride + y * (int64_t)N;
+      for (int k = 0; k < 3; ++k)
+        if (a.maps_mask >> k & 1) bulk_prefetch_l2(M + k * a.maps_plane, N * 4u);
+    }
+  }
+}
+
 // DEEP: every exchange of both transforms in Xs (two barriers each), so Xn
 // is free from the start and the next item's copies are issued right after
 // the lines are read: they are in flight for the whole item, not only for the
@@ -174,6 +207,8 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
       for (int j = 0; j < E; ++j) vpre[j] = __ldg(V1 + va + j * TPL);
     }
   }
+  // the first set's per-field parameters, requested before the transform
+  const NLP2 pset0 = load_nlp2(P, fa, fb, 0);
   __syncthreads();  // every thread has read its lines from buffer st
   float4* sA = reinterpret_cast<float4*>(buf(Xs, 2 * pp));
   float4* sB = reinterpret_cast<float4*>(buf(Xn, 2 * pp));
@@ -186,7 +221,18 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
   // (1/N: applied by the column pass through the blocked propagator)
   // V' = vscale * V rounded in single precision, as the reference's k/2*V array
   auto nl_all = [&](int set) {
-    const NLP2 p0 = load_nlp2(P, fa, fb, set);
+    const NLP2 p0 = set == 0 ? pset0 : load_nlp2(P, fa, fb, set);
+    if (has_v && !VSHARED && !v_cplx && !(a.flags & F_MAPS)) {
+      // a real potential per field: every value of both lines requested
+      // before the first use (one L2 round trip per item, not one per position)
+      const float* V1 = reinterpret_cast<const float*>(a.V);
+      float2 vv[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) vv[j] = f2(__ldg(V1 + va + j * TPL), __ldg(V1 + vb + j * TPL));
+#pragma unroll
+      for (int j = 0; j < E; ++j) x[j] = nl_pair_point(x[j], p0, true, mul2(p0.vs, vv[j]), f2s(0.f));
+      return;
+    }
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       NLP2 p = p0;
@@ -295,6 +341,7 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, RowPair<N, EP>::THREA
       for (int bx = 0; bx < NBOX; ++bx)
         tensor_load_4d(buf(b, (int)l) + bx * BOXB * W, &tmS, 0, (int)y, bx * BOXB, (int)f, &bar[b]);
     }
+    pair_prefetch_inputs<N, EP>(a, g);
   };
   auto prefetch = [&](int b, unsigned gn) {
     if (gn < ngroups) {

@@ -90,6 +90,12 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src_gmem, 
       : "memory");
 }
 
+// Bring `bytes` of global memory into L2 ahead of their loads (no completion
+// to wait for).  src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src_gmem, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
+}
+
 // 4-D tiled tensor-map load into shared memory completing on `bar`; the map
 // lives in kernel parameter space (__grid_constant__).  Coordinate c0 (the
 // innermost) must be a multiple of 16 bytes; it is always 0 here.

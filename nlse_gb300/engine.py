@@ -63,8 +63,10 @@ class Plan:
         self.shape0 = self.shape
 
     @classmethod
-    def get(cls, ndim, shape, nfields, comps, dtype, device) -> "Plan":
-        key = (ndim, tuple(shape), int(nfields), int(comps), int(dtype), str(device))
+    def get(cls, ndim, shape, nfields, comps, dtype, device, slot: int = 0) -> "Plan":
+        """The cached plan of this geometry; slot > 0 gives further plans of the
+        same geometry (each keeps its own captured loop)."""
+        key = (ndim, tuple(shape), int(nfields), int(comps), int(dtype), str(device), int(slot))
         p = cls._cache.get(key)
         if p is None:
             p = cls(ndim, shape, nfields, comps, dtype, device)
@@ -162,17 +164,20 @@ class OperatorData:
     # unique per operator: tells the plan its cached copy of the propagator is stale
     version: int = field(default_factory=lambda: next(_versions))
 
-    def struct(self) -> _lib.Operator:
+    def struct(self, field0: int = 0) -> _lib.Operator:
+        """The C descriptor; field0 > 0 describes fields field0, field0 + 1, ... of
+        the batch the operator was built for (per-field parameters, potentials
+        and coefficient planes start at that field)."""
         o = _lib.Operator()
         if self.V is not None:
-            o.V = self.V.data_ptr()
+            o.V = self.V.data_ptr() + field0 * int(self.v_fstride) * self.V.element_size()
             o.v_complex = int(self.V.is_complex())
             o.v_f32 = int(self.V.dtype in (torch.float32, torch.complex64))
             o.v_fstride = int(self.v_fstride)
         o.prop = self.prop.data_ptr()
         o.prop_c128 = int(self.prop.dtype == torch.complex128)
         o.prop_cstride = int(self.prop_cstride)
-        o.params = self.params.data_ptr()
+        o.params = self.params.data_ptr() + field0 * _lib.NLSE_PARAM_STRIDE * 8
         o.scheme = int(self.scheme)
         o.rabi = int(bool(self.rabi))
         if self.pump is not None:
@@ -185,18 +190,21 @@ class OperatorData:
         if self.nl_khat is not None:
             o.nl_khat = self.nl_khat.data_ptr()
         if self.maps is not None and self.maps_mask:
-            o.nl_maps = self.maps.data_ptr()
             o.maps_plane = int(self.maps.shape[1] * self.maps.shape[2])
             o.maps_fstride = int(self.maps.shape[2]) if self.maps.shape[1] > 1 else 0
+            o.nl_maps = self.maps.data_ptr() + field0 * o.maps_fstride * self.maps.element_size()
             o.maps_mask = int(self.maps_mask)
+        if field0 and self.pump is not None:
+            raise ValueError("a field offset of an operator with pump terms")
         return o
 
 
 def propagate(plan: Plan, A: torch.Tensor, op: OperatorData, nsteps: int, step0: int = 0,
-              graph: bool = False) -> None:
-    """Advance A in place by nsteps split steps (nlse_propagate)."""
+              graph: bool = False, field0: int = 0) -> None:
+    """Advance A in place by nsteps split steps (nlse_propagate); A holds the
+    fields field0, field0 + 1, ... of the batch op was built for."""
     require_cuda(A)
-    s = op.struct()
+    s = op.struct(field0)
     flags = _lib.NLSE_RUN_GRAPH if graph else 0
     with torch.cuda.device(A.device):
         _lib.check(plan.lib.nlse_propagate(plan.handle, A.data_ptr(), ct.byref(s), int(nsteps),

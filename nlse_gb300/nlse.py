@@ -84,6 +84,17 @@ def count_steps(z: float, delta_z) -> int:
     return n
 
 
+_PIPE_STREAMS: dict = {}
+
+
+def _pipeline_streams(dev: torch.device) -> tuple:
+    """The upload and download streams of the host pipeline on one device."""
+    key = str(dev)
+    if key not in _PIPE_STREAMS:
+        _PIPE_STREAMS[key] = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+    return _PIPE_STREAMS[key]
+
+
 class NLSE:
     """A class to solve NLSE"""
 
@@ -450,6 +461,8 @@ class NLSE:
         in_dtype = E_in.dtype
         assert in_dtype in (np.complex64, np.complex128, torch.complex64, torch.complex128), (
             "Type mismatch, E_in should be complex64 or complex128")
+        if callback is None and self._pipeline_chunks(E_in) > 1:
+            return self._out_field_pipelined(E_in, z, precision, verbose, normalize)
         if self.propagator is None:
             self.propagator = self._build_propagator()
         self._send_arrays_to_gpu()
@@ -546,6 +559,109 @@ class NLSE:
         if isinstance(E_in, torch.Tensor) and not E_in.is_cuda:
             return engine.to_host(A)
         return A
+
+    # host batches of at least this size go through the copy/compute pipeline
+    PIPELINE_MIN_BYTES = 64 << 20
+
+    def _pipeline_chunks(self, E_in) -> int:
+        """Chunks of the host-to-host pipeline for this input (1: not pipelined).
+
+        A page-locked host batch of 2-D fields (this class, no nonlocal
+        response) of at least PIPELINE_MIN_BYTES is split by fields: its
+        chunks' uploads, propagations and downloads overlap."""
+        if type(self) is not NLSE or self.nl_length > 0:
+            return 1
+        if not (isinstance(E_in, torch.Tensor) and not E_in.is_cuda and E_in.is_pinned()
+                and E_in.is_contiguous()):
+            return 1
+        lead = self._lead_shape(tuple(E_in.shape))
+        nf = int(np.prod(lead)) if lead else 1
+        if nf < 2 or E_in.numel() * E_in.element_size() < self.PIPELINE_MIN_BYTES:
+            return 1
+        return 4 if nf >= 8 else 2
+
+    def _out_field_pipelined(self, E_in: torch.Tensor, z: float, precision: str, verbose: bool,
+                             normalize: bool) -> torch.Tensor:
+        """out_field of a page-locked host batch with the host link and the
+        device overlapped: the batch is split into field chunks; chunk i is
+        uploaded on one stream, normalised and propagated (its own plan and
+        captured loop) on the current stream, and downloaded into page-locked
+        memory on a third stream while chunk i + 1 is propagated.  Every field
+        is computed exactly as in the unsplit call with the same kernel variant
+        (fields are independent)."""
+        dev = self._device
+        if self.propagator is None:
+            self.propagator = self._build_propagator()
+        self._send_arrays_to_gpu()
+        V = None if self.V is None else self.V.clone()
+        shape = tuple(E_in.shape)
+        lead = self._lead_shape(shape)
+        nf = int(np.prod(lead))
+        grid = shape[len(lead):]
+        nchunks = self._pipeline_chunks(E_in)
+        bounds = [nf * i // nchunks for i in range(nchunks + 1)]
+        host_in = E_in.reshape(nf, *grid)
+        A = torch.empty((nf, *grid), dtype=E_in.dtype, device=dev)
+        stage = torch.empty_like(A) if normalize else A
+        out = torch.empty((nf, *grid), dtype=E_in.dtype, pin_memory=True)
+        dtype = engine.dtype_code(A)
+        plans = [Plan.get(2, grid, b1 - b0, 1, dtype, dev, slot=i)
+                 for i, (b0, b1) in enumerate(zip(bounds, bounds[1:]))]
+        cur = torch.cuda.current_stream(dev)
+        s_in, s_out = _pipeline_streams(dev)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(cur)
+        t0 = time.perf_counter()
+        n2_old = self.n2
+        try:
+            if z > self.L:
+                self.n2 = 0
+            n = count_steps(z, self.delta_z)
+            op = self._operator(A, V, self.propagator, precision, None, plans[0])
+            target = None
+            if normalize:
+                target = torch.from_numpy(np.array(self._norm_target(lead), dtype=np.float64)
+                                          .reshape(-1)).to(dev)
+            # uploads: all chunks back to back on s_in, after this stream's set-up
+            s_in.wait_stream(cur)
+            loaded = []
+            with torch.cuda.stream(s_in):
+                for b0, b1 in zip(bounds, bounds[1:]):
+                    stage[b0:b1].copy_(host_in[b0:b1], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(s_in)
+                    loaded.append(ev)
+            for i, (b0, b1) in enumerate(zip(bounds, bounds[1:])):
+                cur.wait_event(loaded[i])
+                Ac = A[b0:b1]
+                if normalize:
+                    sums = engine.power(stage[b0:b1], b1 - b0)
+                    engine.normalize(stage[b0:b1], Ac, b1 - b0, sums, target[b0:b1],
+                                     self._norm_coef())
+                if n > 0:
+                    if i == 0:
+                        autotune.maybe_tune(plans[0], Ac, op)
+                    else:
+                        # every chunk runs the first chunk's kernel variant
+                        v = plans[0].get_variant()
+                        plans[i].set_variant(v["rows"], v["cols"], v["rows_cap"], v["cols_cap"])
+                    engine.propagate(plans[i], Ac, op, n, 0, graph=True, field0=b0)
+                done = torch.cuda.Event()
+                done.record(cur)
+                s_out.wait_event(done)
+                with torch.cuda.stream(s_out):
+                    out[b0:b1].copy_(Ac, non_blocking=True)
+            cur.wait_stream(s_out)
+        finally:
+            self.n2 = n2_old
+        end.record(cur)
+        end.synchronize()
+        if verbose:
+            print(f"\nTime spent to solve : {start.elapsed_time(end) * 1e-3} s (GPU) /"
+                  f" {time.perf_counter() - t0} s (CPU)\n")
+        self._retrieve_arrays_from_gpu()
+        return out.reshape(shape)
 
     def _op_key(self):
         """Snapshot of the attributes the operator depends on (callbacks may change them)."""

@@ -27,12 +27,36 @@ def rel_l2(a, b) -> float:
     return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
 
 
+_LN2_HI = 6.93147180369123816490e-01  # ln 2 split for Cody-Waite reduction
+_LN2_LO = 1.90821492927058770002e-10
+
+
+def portable_exp(x):
+    """exp of a float array, evaluated in float64 with IEEE +, -, *, / and
+    ldexp only, so the same bits on every machine.  Library exp differs in
+    its last bit between x86 and Arm NumPy builds, and the full-size
+    workloads (2048^2, 501 steps) carry such input differences through to
+    ~1e-7 in their outputs; fixtures made on one machine are replayed on the
+    other.  Cody-Waite reduction x = k ln2 + r, |r| <= ln2 / 2, and the
+    degree-13 Taylor polynomial of exp(r) (truncation below 1e-17)."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * 1.4426950408889634)  # x / ln 2
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.ones_like(r)
+    for n in range(13, 0, -1):
+        p = 1.0 + p * r / n
+    out = np.ldexp(p, np.clip(k, -1100, 1100).astype(np.int64))
+    return np.where(x < -745.0, 0.0, out)
+
+
 def gaussian(XX, YY, w=WAIST):
-    return np.exp(-(XX**2 + YY**2) / w**2)
+    XX, YY = np.asarray(XX, np.float64), np.asarray(YY, np.float64)
+    return portable_exp(-(XX**2 + YY**2) / w**2)
 
 
 def potential(XX, YY):
-    return -1e-4 * np.exp(-(XX**2 + YY**2) / WAIST2**2)
+    XX, YY = np.asarray(XX, np.float64), np.asarray(YY, np.float64)
+    return -1e-4 * portable_exp(-(XX**2 + YY**2) / WAIST2**2)
 
 
 def nlse_beam(cls, N, dtype=np.complex64, noise=0.0, seed=0, with_v=True, dz=5e-5, batch=None,
@@ -96,9 +120,12 @@ def mixed_batch(groups, seed=0, dtype=np.complex64, cls=None, dz=5e-5):
                 depth = rng.uniform(0.5e-4, 2e-4)
                 width = rng.uniform(30e-6, 150e-6)
                 x0, y0 = rng.uniform(-WINDOW / 4, WINDOW / 4, 2)
-                V[b] -= depth * np.exp(-((sim.XX - x0) ** 2 + (sim.YY - y0) ** 2) / width**2)
+                dx = np.asarray(sim.XX, np.float64) - x0
+                dy = np.asarray(sim.YY, np.float64) - y0
+                V[b] -= depth * portable_exp(-(dx**2 + dy**2) / width**2)
         sim.V = V.astype(np.float32)
-        E = np.exp(-(sim.XX[None] ** 2 + sim.YY[None] ** 2) / waist[:, None, None] ** 2)
+        r2 = np.asarray(sim.XX, np.float64) ** 2 + np.asarray(sim.YY, np.float64) ** 2
+        E = portable_exp(-r2[None] / waist[:, None, None] ** 2)
         jobs.append((sim, E.astype(dtype)))
     return jobs
 
@@ -130,7 +157,7 @@ def cnlse1024_inputs(cls, dtype, N=1024):
     sim.power2 = 0.05
     sim.n22 = N2
     r = np.arange(-33, 34) * sim.delta_X
-    kern = np.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * (100e-6) ** 2))
+    kern = portable_exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * (100e-6) ** 2))
     sim.nl_profile = kern / kern.sum()
     E = np.array([gaussian(sim.XX, sim.YY, w) for w in (1.5e-3, 0.5e-3)])
     return sim, E.astype(dtype)
