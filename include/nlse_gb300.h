@@ -192,15 +192,16 @@ int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
  *         packed FP32: complex64, columns of 64..2048 points).
  *   NLSE_ROWS_DEEP / NLSE_COLS_DEEP: the pair passes with deeper prefetch
  *         (the next work item's copies in flight during the whole current
- *         item; rows: exchanges in the item's own buffer, columns: three
+ *         item; rows: exchanges in the item's own buffer and the mid-loop
+ *         pass's rows stored by tensor map from shared memory, columns: three
  *         staging tiles and no exchange tile), same sizes as the pair ones.
  * rows_ctas_per_sm / cols_ctas_per_sm cap the persistent passes' CTAs per SM
  * (0: as many as fit), which sets their grid (SMs x CTAs per SM).  A launch
  * the chosen variant cannot serve (two components, Rabi or pump terms, a
  * complex128 propagator, an external |A|^2) runs the TMA variant instead.
  * get returns the current choice and bit masks of the available variants
- * (bit v set: variant code v).  The plan's default is the pair variants
- * where available, else the TMA ones.  No reference counterpart (the
+ * (bit v set: variant code v).  The plan's default is NLSE_ROWS_DEEP and
+ * NLSE_COLS_PAIR where available, else the TMA variants.  No reference counterpart (the
  * reference's VkFFTApp(tune=True) tunes its FFT plan, NLSE/nlse.py:216);
  * nlse_gb300.autotune searches these. */
 #define NLSE_ROWS_LINE 0

@@ -725,7 +725,7 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     if (p->cols_tma_ok) p->cols_avail |= 1u << NLSE_COLS_TMA;
     if (p->cols_tma_ok && pair && p->lg[0] >= 6 && p->lg[0] <= 11)
       p->cols_avail |= (1u << NLSE_COLS_PAIR) | (1u << NLSE_COLS_PAIR8) | (1u << NLSE_COLS_DEEP);
-    p->rows_var = (p->rows_avail >> NLSE_ROWS_PAIR & 1) ? NLSE_ROWS_PAIR
+    p->rows_var = (p->rows_avail >> NLSE_ROWS_DEEP & 1) ? NLSE_ROWS_DEEP
                   : p->rows_tma                          ? NLSE_ROWS_TMA
                                                          : NLSE_ROWS_LINE;
     p->cols_var = (p->cols_avail >> NLSE_COLS_PAIR & 1) ? NLSE_COLS_PAIR

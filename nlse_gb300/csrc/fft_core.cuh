@@ -60,6 +60,10 @@ __device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// c - a * b
+__device__ __forceinline__ float2 fnma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, make_float2(-b.x, -b.y), c);
+}
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   unsigned long long r;
   asm("sub.rn.f32x2 %0, %1, %2;"
@@ -68,6 +72,12 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
         "l"(*reinterpret_cast<const unsigned long long*>(&b)));
   return *reinterpret_cast<const float2*>(&r);
 }
+
+// Two complex64 values, lane-wise: re = (a.re, b.re), im = (a.im, b.im) (two
+// lines at one position, or two positions of one line).
+struct __align__(16) cp2 {
+  float2 re, im;
+};
 
 // Complex sums and differences; a complex64 value {re, im} is one register
 // pair, so these are single packed instructions (same results as two scalar
@@ -110,7 +120,12 @@ __device__ __forceinline__ cpx<T> mul_mi(cpx<T> a) {
 template <typename T, bool INV>
 __device__ __forceinline__ cpx<T> mul_w(cpx<T> a, T wr, T wi) {
   const T s = INV ? wi : -wi;
-  return mk<T>(a.x * wr - a.y * s, a.x * s + a.y * wr);
+  if constexpr (sizeof(T) == 4) {
+    // (re, im) = a.x (wr, s) + a.y (-s, wr): two packed instructions
+    return fma2(f2s(a.y), f2(-s, wr), mul2(f2s(a.x), f2(wr, s)));
+  } else {
+    return mk<T>(a.x * wr - a.y * s, a.x * s + a.y * wr);
+  }
 }
 
 // cos(pi/8), sin(pi/8), sqrt(1/2)

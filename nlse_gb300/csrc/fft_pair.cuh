@@ -23,14 +23,6 @@
 
 namespace nlse {
 
-struct __align__(16) cp2 {
-  float2 re, im;
-};
-
-// c - a * b
-__device__ __forceinline__ float2 fnma2(float2 a, float2 b, float2 c) {
-  return __ffma2_rn(a, make_float2(-b.x, -b.y), c);
-}
 
 __device__ __forceinline__ cp2 pcadd(cp2 a, cp2 b) { return {add2(a.re, b.re), add2(a.im, b.im)}; }
 __device__ __forceinline__ cp2 pcsub(cp2 a, cp2 b) { return {sub2(a.re, b.re), sub2(a.im, b.im)}; }

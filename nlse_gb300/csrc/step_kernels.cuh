@@ -254,6 +254,73 @@ __device__ __forceinline__ cpx<T> nl_point(cpx<T> A, T a_s, T a_c, const NLP<T>&
   return cmul<T>(A, mk<T>(cr, ci));
 }
 
+// Parameters of one nonlinear sub-step on two lanes (two lines, or two
+// positions of one line: then both lanes hold the same values).
+struct NLP2 {
+  float2 dz, nalpha, gs, ris, vs, dzi;
+  bool real_dz;
+};
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// exp(re) * (cos(im), sin(im)) for both lanes: the truncated series of
+// cis_exp in packed form, the library functions for a
+// lane outside the series' range.
+__device__ __forceinline__ void pcis_exp(float2 re, float2 im, float2* cr, float2* ci) {
+  using R = CisRange<float>;
+  float2 e = f2s(float(inv_fact(R::EXP_DEG)));
+#pragma unroll
+  for (int k = R::EXP_DEG - 1; k >= 0; --k) e = fma2(e, re, f2s(float(inv_fact(k))));
+  const float2 x2 = mul2(im, im);
+  float2 s = f2s(float(sin_coef(R::SIN_K)));
+#pragma unroll
+  for (int k = R::SIN_K - 1; k >= 1; --k) s = fma2(s, x2, f2s(float(sin_coef(k))));
+  const float2 sn = fma2(mul2(im, x2), s, im);
+  float2 c = f2s(float(cos_coef(R::COS_K)));
+#pragma unroll
+  for (int k = R::COS_K - 1; k >= 0; --k) c = fma2(c, x2, f2s(float(cos_coef(k))));
+  *cr = mul2(e, c);
+  *ci = mul2(e, sn);
+  const bool ina = fabsf(re.x) <= R::RE && fabsf(im.x) <= R::IM;
+  const bool inb = fabsf(re.y) <= R::RE && fabsf(im.y) <= R::IM;
+  if (!(ina && inb)) {
+    if (!ina) cis_exp_lib(re.x, im.x, &cr->x, &ci->x);
+    if (!inb) cis_exp_lib(re.y, im.y, &cr->y, &ci->y);
+  }
+}
+
+// One nonlinear sub-step on one pair point; v = vscale * V of each lane
+// (v.x/v.y = real parts, vi = imaginary parts or zero).
+__device__ __forceinline__ cp2 nl_pair_point(cp2 x, const NLP2& p, bool has_v, float2 vre,
+                                             float2 vim) {
+  const float2 one = f2s(1.0f);
+  const float2 as = fma2(x.re, x.re, mul2(x.im, x.im));
+  const float2 den = fma2(as, p.ris, one);
+  float2 sat = f2(rcp_approx(den.x), rcp_approx(den.y));
+  sat = fma2(sat, fnma2(den, sat, one), sat);  // one Newton step
+  float2 im = mul2(mul2(p.gs, as), sat);
+  float2 re = mul2(p.nalpha, sat);
+  if (has_v) {
+    re = sub2(re, vim);
+    im = add2(im, vre);
+  }
+  float2 ar, ai;
+  if (p.real_dz) {
+    ar = mul2(re, p.dz);
+    ai = mul2(im, p.dz);
+  } else {
+    ar = fnma2(im, p.dzi, mul2(re, p.dz));
+    ai = fma2(re, p.dzi, mul2(im, p.dz));
+  }
+  float2 cr, ci;
+  pcis_exp(ar, ai, &cr, &ci);
+  return {fnma2(x.im, ci, mul2(x.re, cr)), fma2(x.re, ci, mul2(x.im, cr))};
+}
+
 template <typename T>
 __device__ __forceinline__ T inv_n_of(const StepArgs& a) {
   if constexpr (std::is_same<T, float>::value) return a.inv_nf;

@@ -121,12 +121,17 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
   }
   __syncthreads();
   if (threadIdx.x == 0 && blockIdx.x < m.items) issue(0, blockIdx.x);
+  // the deep item form (the next item's copies issued at the item's start) with
+  // the mid-loop pass's rows stored by tensor map from shared memory
+  constexpr bool TST = MODE == ROW_INV_NL_FWD;
   int it = 0;
   for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
     const int st = it & 1;
     const unsigned par = (it >> 1) & 1;
     const int k = multi_plan_of(item, m);
     const StepArgs& a = m.p[k].a;
+    // the previous item's row stores have read the buffer the next copy fills
+    if (TST && threadIdx.x == 0) bulk_wait_read_all();
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
       if (threadIdx.x == 0) {
@@ -144,13 +149,15 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
         issue(st ^ 1, next);
       }
     };
+    const CUtensorMap* tms = TST ? &m.tm[k] : nullptr;
     switch (m.p[k].log2n) {
-      case 8: pair_row_item<256, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
-      case 9: pair_row_item<512, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
-      case 10: pair_row_item<1024, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
-      default: pair_row_item<2048, 16, MODE, false>(a, g, Xs, Xn, prefetch); break;
+      case 8: pair_row_item<256, 16, MODE, false, true>(a, g, Xs, Xn, prefetch, tms); break;
+      case 9: pair_row_item<512, 16, MODE, false, true>(a, g, Xs, Xn, prefetch, tms); break;
+      case 10: pair_row_item<1024, 16, MODE, false, true>(a, g, Xs, Xn, prefetch, tms); break;
+      default: pair_row_item<2048, 16, MODE, false, true>(a, g, Xs, Xn, prefetch, tms); break;
     }
   }
+  if (TST && threadIdx.x == 0) bulk_wait_all();
 }
 
 // ---- column pass ------------------------------------------------------------

@@ -19,12 +19,6 @@
 
 namespace nlse {
 
-// Per-line parameters of one nonlinear sub-step, lanes = (line a, line b).
-struct NLP2 {
-  float2 dz, nalpha, gs, ris, vs, dzi;
-  bool real_dz;
-};
-
 __device__ __forceinline__ NLP2 load_nlp2(const float* __restrict__ P, int64_t fa, int64_t fb,
                                           int set) {
   const float* pa = P + fa * kParamStride;
@@ -38,66 +32,6 @@ __device__ __forceinline__ NLP2 load_nlp2(const float* __restrict__ P, int64_t f
   r.dzi = f2(__ldg(pa + 32 + set), __ldg(pb + 32 + set));
   r.real_dz = r.dzi.x == 0.0f && r.dzi.y == 0.0f;
   return r;
-}
-
-__device__ __forceinline__ float rcp_approx(float x) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
-// exp(re) * (cos(im), sin(im)) for both lanes: the truncated series of
-// cis_exp (step_kernels.cuh) in packed form, the library functions for a
-// lane outside the series' range.
-__device__ __forceinline__ void pcis_exp(float2 re, float2 im, float2* cr, float2* ci) {
-  using R = CisRange<float>;
-  float2 e = f2s(float(inv_fact(R::EXP_DEG)));
-#pragma unroll
-  for (int k = R::EXP_DEG - 1; k >= 0; --k) e = fma2(e, re, f2s(float(inv_fact(k))));
-  const float2 x2 = mul2(im, im);
-  float2 s = f2s(float(sin_coef(R::SIN_K)));
-#pragma unroll
-  for (int k = R::SIN_K - 1; k >= 1; --k) s = fma2(s, x2, f2s(float(sin_coef(k))));
-  const float2 sn = fma2(mul2(im, x2), s, im);
-  float2 c = f2s(float(cos_coef(R::COS_K)));
-#pragma unroll
-  for (int k = R::COS_K - 1; k >= 0; --k) c = fma2(c, x2, f2s(float(cos_coef(k))));
-  *cr = mul2(e, c);
-  *ci = mul2(e, sn);
-  const bool ina = fabsf(re.x) <= R::RE && fabsf(im.x) <= R::IM;
-  const bool inb = fabsf(re.y) <= R::RE && fabsf(im.y) <= R::IM;
-  if (!(ina && inb)) {
-    if (!ina) cis_exp_lib(re.x, im.x, &cr->x, &ci->x);
-    if (!inb) cis_exp_lib(re.y, im.y, &cr->y, &ci->y);
-  }
-}
-
-// One nonlinear sub-step on one pair point; v = vscale * V of each lane
-// (v.x/v.y = real parts, vi = imaginary parts or zero).
-__device__ __forceinline__ cp2 nl_pair_point(cp2 x, const NLP2& p, bool has_v, float2 vre,
-                                             float2 vim) {
-  const float2 one = f2s(1.0f);
-  const float2 as = fma2(x.re, x.re, mul2(x.im, x.im));
-  const float2 den = fma2(as, p.ris, one);
-  float2 sat = f2(rcp_approx(den.x), rcp_approx(den.y));
-  sat = fma2(sat, fnma2(den, sat, one), sat);  // one Newton step
-  float2 im = mul2(mul2(p.gs, as), sat);
-  float2 re = mul2(p.nalpha, sat);
-  if (has_v) {
-    re = sub2(re, vim);
-    im = add2(im, vre);
-  }
-  float2 ar, ai;
-  if (p.real_dz) {
-    ar = mul2(re, p.dz);
-    ai = mul2(im, p.dz);
-  } else {
-    ar = fnma2(im, p.dzi, mul2(re, p.dz));
-    ai = fma2(re, p.dzi, mul2(im, p.dz));
-  }
-  float2 cr, ci;
-  pcis_exp(ar, ai, &cr, &ci);
-  return {fnma2(x.im, ci, mul2(x.re, cr)), fma2(x.re, ci, mul2(x.im, cr))};
 }
 
 // Shape of the pair row pass: EP positions per thread and line (16, or 8 for
@@ -159,9 +93,14 @@ __device__ __forceinline__ void pair_prefetch_inputs(const StepArgs& a, unsigned
 // is free from the start and the next item's copies are issued right after
 // the lines are read: they are in flight for the whole item, not only for the
 // forward transform (twice the bytes in flight per CTA over an item).
+// tms (mid-loop pass): the item's lines leave through shared memory and
+// tensor-map stores issued by thread 0 instead of 8-byte stores per thread
+// (a quarter of the L1 store wavefronts; the caller waits for the stores'
+// reads before the buffer is written again); nullptr: direct stores.
 template <int N, int EP, int MODE, bool VSHARED, bool DEEP = false, typename Prefetch>
 __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, float2* Xs,
-                                              float2* Xn, Prefetch&& prefetch) {
+                                              float2* Xn, Prefetch&& prefetch,
+                                              const CUtensorMap* tms = nullptr) {
   using RP = RowPair<N, EP>;
   using C = float2;
   constexpr int E = RP::E, TPL = RP::TPL, W = BlkW<float>::W, LPC = RP::LPC, SLS = RP::SLS;
@@ -272,7 +211,32 @@ __device__ __forceinline__ void pair_row_item(const StepArgs& a, unsigned g, flo
         if (threadIdx.x == 0) prefetch();
       });
     }
-    if (act) {
+    if (tms) {
+      // the rows in natural order in this item's buffer (a row of the blocked
+      // layout is its runs of W elements back to back: one tensor-map box)
+      constexpr int NB = N / W, BOXB = NB < 256 ? NB : 256, NBOX = NB / BOXB;
+      __syncthreads();  // every exchange read of the buffer is complete
+      C* la = buf(Xs, 2 * pp);
+      C* lb = buf(Xs, 2 * pp + 1);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        la[t + j * TPL] = f2(x[j].re.x, x[j].im.x);
+        lb[t + j * TPL] = f2(x[j].re.y, x[j].im.y);
+      }
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned q0 = g * LPC;
+        const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+        for (unsigned l = 0; l < nl; ++l) {
+          const unsigned q = q0 + l;
+#pragma unroll
+          for (int bx = 0; bx < NBOX; ++bx)
+            tensor_store_4d(tms, 0, (int)q_y(q), bx * BOXB, (int)q_f(q), buf(Xs, (int)l) + bx * BOXB * W);
+        }
+        bulk_commit_group();
+      }
+    } else if (act) {
       const int64_t lpc = a.lines_per_comp, dstr = (int64_t)TPL * lpc;
       C* da = reinterpret_cast<C*>(a.S) + fa * a.pix + ((t / W) * lpc + ma) * W + (t % W);
       C* db = reinterpret_cast<C*>(a.S) + fb * a.pix + ((t / W) * lpc + mb) * W + (t % W);
@@ -355,10 +319,15 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, RowPair<N, EP>::THREA
   }
   __syncthreads();
   if (threadIdx.x == 0 && blockIdx.x < ngroups) issue(0, blockIdx.x);
+  // the deep form stores the mid-loop pass's rows by tensor map from shared memory
+  constexpr bool TST = DEEP && MODE == ROW_INV_NL_FWD;
   int it = 0;
   for (unsigned g = blockIdx.x; g < ngroups; g += gridDim.x, ++it) {
     const int st = it & 1;
     const unsigned par = (it >> 1) & 1;
+    // the previous item's row stores have read the buffer it leaves behind
+    // (written again below: exchanges or the next copy)
+    if (TST && threadIdx.x == 0) bulk_wait_read_all();
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
       if (threadIdx.x == 0) {
@@ -367,10 +336,11 @@ __global__ void __launch_bounds__(RowPair<N, EP>::THREADS, RowPair<N, EP>::THREA
       }
       return;
     }
-    pair_row_item<N, EP, MODE, VSHARED, DEEP>(a, g, buf(st, 0), buf(st ^ 1, 0), [&] {
-      prefetch(st ^ 1, g + gridDim.x);
-    });
+    pair_row_item<N, EP, MODE, VSHARED, DEEP>(
+        a, g, buf(st, 0), buf(st ^ 1, 0), [&] { prefetch(st ^ 1, g + gridDim.x); },
+        TST ? &tmS : nullptr);
   }
+  if (TST && threadIdx.x == 0) bulk_wait_all();
 }
 
 }  // namespace nlse

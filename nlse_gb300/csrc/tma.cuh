@@ -90,6 +90,30 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src_gmem, 
       : "memory");
 }
 
+// 4-D tiled tensor-map store of a shared-memory box (128-byte aligned source)
+// into global memory, in the calling thread's bulk group.  The box's shared
+// writes must be fenced (fence_proxy_async_smem by every writer, then a
+// barrier) before the store is issued.
+__device__ __forceinline__ void tensor_store_4d(const CUtensorMap* map, int c0, int c1, int c2,
+                                                int c3, const void* src_smem) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src_smem))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit_group() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// every committed store of this thread has finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// every committed store of this thread is complete in global memory
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 // Bring `bytes` of global memory into L2 ahead of their loads (no completion
 // to wait for).  src 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src_gmem, unsigned bytes) {
