@@ -1,7 +1,9 @@
 """out_field on a page-locked host batch: the pipelined path (uploads,
 propagations and downloads of field chunks overlapped) against the same call
-on device input.  Fields are independent and every chunk runs the kernel
-variant of the first, so the results are bit-identical."""
+on device input.  Fields are independent, so with the same kernel variant
+the results are bit-identical; the chunks' plans are other geometries than
+the whole batch's, and left to their own (tuned) variants they agree to
+complex64 rounding."""
 
 import numpy as np
 import pytest
@@ -10,6 +12,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 import nlse_gb300 as ng  # noqa: E402
+from nlse_gb300 import _lib, engine  # noqa: E402
 from tests import cases  # noqa: E402
 
 
@@ -38,11 +41,24 @@ def test_pipelined_host_batch_equals_device_call(N, B, per_field, chunks, monkey
     sim, E = _sim(N, B, per_field, N + B)
     Eh = torch.from_numpy(E).pin_memory()
     assert sim._pipeline_chunks(Eh) == chunks
+    # every plan involved on one variant: the pipelined fields are the unsplit call's
+    dev = torch.device("cuda", 0)
+    bounds = [B * i // chunks for i in range(chunks + 1)]
+    plans = [engine.Plan.get(2, (N, N), b1 - b0, 1, _lib.NLSE_C64, dev, slot=i)
+             for i, (b0, b1) in enumerate(zip(bounds, bounds[1:]))]
+    plans.append(engine.Plan.get(2, (N, N), B, 1, _lib.NLSE_C64, dev))
+    for p in plans:
+        p.set_variant(_lib.ROWS_DEEP, _lib.COLS_PAIR)
     got = sim.out_field(Eh, z, verbose=False)
     assert isinstance(got, torch.Tensor) and not got.is_cuda and got.shape == Eh.shape
     sim2, _ = _sim(N, B, per_field, N + B)
     ref = sim2.out_field(torch.from_numpy(E).cuda(), z, verbose=False).cpu()
     assert torch.equal(got, ref)
+    # the chunks on another variant than the whole batch: complex64 rounding apart
+    for p in plans[:-1]:
+        p.set_variant(_lib.ROWS_TMA, _lib.COLS_TILE)
+    other = sim.out_field(Eh, z, verbose=False)
+    assert cases.rel_l2(other.numpy(), ref.numpy()) <= 1e-5
     # a pageable NumPy batch takes the unsplit path and agrees as well
     assert sim._pipeline_chunks(E) == 1
     np.testing.assert_array_equal(sim.out_field(E, z, verbose=False), ref.numpy())
