@@ -819,7 +819,7 @@ int enqueue_group_fused(int n, const nlse_plan* plans, void* const* fields,
   }
   const int nsm = plans[0]->nsm;
   for (int64_t st = 0; st < nsteps; ++st) {
-    cudaError_t e = launch_cols_multi(n, col.data(), lc.data(), nsm, s, false);
+    cudaError_t e = launch_cols_tile_multi(n, col.data(), lc.data(), s, false);
     if (e != cudaSuccess) return cuda_fail(e, "column pass (all plans)");
     if (st + 1 < nsteps)
       e = launch_rows_multi(ROW_INV_NL_FWD, n, mid.data(), tm.data(), lr.data(), nsm, s, false);
@@ -852,7 +852,7 @@ int nlse_group_create(nlse_group* out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
   // kernel attributes of the one-launch-per-pass kernels (outside any capture)
   if (e == cudaSuccess) e = launch_rows_multi(0, 0, nullptr, nullptr, nullptr, 0, nullptr, true);
-  if (e == cudaSuccess) e = launch_cols_multi(0, nullptr, nullptr, 0, nullptr, true);
+  if (e == cudaSuccess) e = launch_cols_tile_multi(0, nullptr, nullptr, nullptr, true);
   if (e != cudaSuccess) {
     nlse_group_destroy(g);
     return cuda_fail(e, "group create");

@@ -44,10 +44,13 @@ cudaError_t launch_cols_pair(int log2n, const ColArgs& a, cudaStream_t s, bool p
 // blocked buffer) and tensor map.  Columns: each plan's blocked column
 // arguments.  nsm: SMs of the device.  prepare_only: set kernel attributes.
 int multi_max_plans();
+// Columns: the blocked column pass of every plan in tile form (one 512-thread
+// CTA per 2048/N tiles of a plan, no persistence; k_cols_blk's arithmetic).
+cudaError_t launch_cols_tile_multi(int n, const ColArgs* c, const int* log2n, cudaStream_t s,
+                                   bool prepare_only);
 cudaError_t launch_rows_multi(int mode, int n, const StepArgs* a, const CUtensorMap* const* tm,
                               const int* log2n, int nsm, cudaStream_t s, bool prepare_only);
-cudaError_t launch_cols_multi(int n, const ColArgs* c, const int* log2n, int nsm, cudaStream_t s,
-                              bool prepare_only);
+
 
 // Pointwise kernels (pointwise.cu).
 int power_chunks(int64_t seg_len);  // partial sums per segment of the power reduction

@@ -40,12 +40,11 @@ cudaError_t launch_rows_multi(int mode, int n, const StepArgs* a, const CUtensor
   return mode == ROW_INV_NL ? rows_multi_last(m, nsm, s, false) : rows_multi_mid(m, nsm, s, false);
 }
 
-cudaError_t launch_cols_multi(int n, const ColArgs* c, const int* log2n, int nsm, cudaStream_t s,
-                              bool prep) {
-  constexpr size_t smem = cols_multi_smem();
-  static_assert(smem <= 227 * 1024, "multi column pass shared memory");
+cudaError_t launch_cols_tile_multi(int n, const ColArgs* c, const int* log2n, cudaStream_t s,
+                                   bool prep) {
+  constexpr size_t smem = kMultiTileSmem;
   if (prep)
-    return cudaFuncSetAttribute(k_cols_pair_multi<>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_cols_tile_multi<>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
   if (n < 1 || n > kMultiMax) return cudaErrorInvalidValue;
   ColMulti m;
@@ -63,9 +62,7 @@ cudaError_t launch_cols_multi(int n, const ColArgs* c, const int* log2n, int nsm
   m.nplans = n;
   m.items = items;
   if (!items) return cudaSuccess;
-  unsigned grid = (unsigned)nsm;
-  if (grid > items) grid = items;
-  k_cols_pair_multi<><<<grid, 256, smem, s>>>(m);
+  k_cols_tile_multi<><<<items, kMultiTileThreads, smem, s>>>(m);
   return cudaGetLastError();
 }
 

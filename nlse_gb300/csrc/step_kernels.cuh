@@ -817,7 +817,10 @@ __global__ void __launch_bounds__(BlkW<T>::W * (N / E)) k_cols_blk(const ColArgs
   C* sm = reinterpret_cast<C*>(smraw);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const int c = threadIdx.x % W, t = threadIdx.x / W;
-  const int64_t b = blockIdx.x % a.ncb, o = blockIdx.x / a.ncb;
+  // tiles field-fastest: the fields of one column block run together, so its
+  // propagator tile is read from HBM once and from L2 by the other fields
+  const int64_t nouter = a.nblocks / a.ncb;
+  const int64_t o = blockIdx.x % nouter, b = blockIdx.x / nouter;
   const int64_t toff = b * (int64_t)(N * W) + t * W + c;
   C* base = reinterpret_cast<C*>(a.A) + o * a.outer_stride + toff;
   C x[E];

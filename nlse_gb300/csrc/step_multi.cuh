@@ -6,14 +6,13 @@
 //   k_rows_pair_multi  item = the LPC pixel-lines of one pair row-pass group
 //                      of one plan (128 threads and the same 2 x 34.8 KB of
 //                      shared memory at every grid size from 256 to 2048);
-//   k_cols_pair_multi  item = 2048/N column tiles of one plan, side by side
-//                      (256 threads: 2 * N/16 per tile; the same 3 x 69.6 KB
-//                      of shared memory at every size).
-// Persistent CTAs take items blockIdx.x, blockIdx.x + gridDim.x, ...; the next
-// item's copies (possibly another plan's) are issued while the current item
-// is transformed, as in the single-plan pair passes (step_pair.cuh), whose
-// arithmetic this is: pair_row_item is shared, the column item repeats
-// k_cols_pair_tma's body per tile.  Every wait is bounded.
+//   k_cols_tile_multi  item = 2048/N blocked column tiles of one plan, side
+//                      by side (512 threads: W * N/16 per tile; one CTA per
+//                      item, no persistence, as k_cols_blk).
+// The row pass's persistent CTAs take items blockIdx.x, blockIdx.x +
+// gridDim.x, ...; the next item's copies (possibly another plan's) are issued
+// at the start of the current item (the deep form of step_pair.cuh, whose
+// pair_row_item this shares).  Every wait is bounded.
 #pragma once
 #include "step_pair.cuh"
 
@@ -160,9 +159,7 @@ __global__ void __launch_bounds__(128, 3) k_rows_pair_multi(const __grid_constan
   if (TST && threadIdx.x == 0) bulk_wait_all();
 }
 
-// ---- column pass ------------------------------------------------------------
-constexpr int kMultiColTile = stage_len<float>(padded_len(2048) * BlkW<float>::W);  // one stage
-
+// ---- column pass --------------------------------------------------------------
 struct ColPlanArgs {
   ColArgs c;      // the plan's blocked column arguments (S, blocked propagator)
   unsigned items; // its items (2048/N tiles each)
@@ -176,138 +173,63 @@ struct ColMulti {
   unsigned items;
 };
 
-__host__ __device__ constexpr size_t cols_multi_smem() {
-  return (size_t)(kColStages + 1) * kMultiColTile * sizeof(float2) + kColStages * sizeof(uint64_t);
-}
+// ---- column pass, tile form ------------------------------------------------
+// One CTA of 512 threads per work item, no persistence: an item is 2048/N
+// blocked tiles of one plan (W columns x N rows each, W * N/16 threads per
+// tile), loaded straight from global memory, transformed with the scalar FFT
+// (packed complex sums), multiplied by the blocked propagator and transformed
+// back -- k_cols_blk's arithmetic.  Many resident warps instead of a copy
+// ring hide the latency.
+constexpr int kMultiTileThreads = BlkW<float>::W * (2048 / 16);
+constexpr int kMultiTileSmem = padded_len(2048) * BlkW<float>::W * (int)sizeof(float2);
 
-// One item of the column pass: sub = 2048/N tiles, tile s handled by threads
-// [s * 2 TPL, (s + 1) * 2 TPL); the same arithmetic as k_cols_pair_tma.
-// Returns after refilling stage st (thread 0 calls refill()).
-template <int N, typename Refill>
-__device__ __forceinline__ void pair_col_item(const ColArgs& c, unsigned g, float2* stage_st,
-                                              float2* xch, Refill&& refill) {
+template <int N>
+__device__ __forceinline__ void tile_col_item(const ColArgs& c, unsigned g, float2* smem) {
   using C = float2;
-  constexpr int E = 16, TPL = N / E, W = BlkW<float>::W, TILE = N * W;
-  constexpr int SLW = stage_len<float>(padded_len(N) * W), SUB = 2048 / N;
-  static_assert(SLW * SUB == kMultiColTile, "sub-tiles fill one stage");
-  constexpr int NEX = fft_exchanges(N, E);
-  static_assert(NEX >= 1, "column transforms exchange at least once");
-  const int s = threadIdx.x / (2 * TPL), lt = threadIdx.x % (2 * TPL);
-  const int p = lt & 1, t = lt >> 1;
-  const int64_t nouter = c.nblocks / c.ncb;
+  constexpr int E = 16, TPL = N / E, W = BlkW<float>::W, THR = W * TPL, SUB = 2048 / N;
+  constexpr int SLT = padded_len(N) * W;  // one tile's exchange buffer
+  static_assert(THR * SUB == kMultiTileThreads, "sub-tiles fill the CTA");
+  static_assert(SLT * SUB * (int)sizeof(C) <= kMultiTileSmem, "sub-tile buffers fit");
+  const int s = threadIdx.x / THR, lt = threadIdx.x % THR;
+  const int cc = lt % W, t = lt / W;
   const int64_t ti = (int64_t)g * SUB + s;
   const bool act = ti < c.nblocks;
   const int64_t tc = act ? ti : c.nblocks - 1;
-  const int64_t o = tc % nouter, b = tc / nouter;
+  // a CTA's sub-tiles are adjacent column blocks of one field (contiguous)
+  const int64_t b = tc % c.ncb, o = tc / c.ncb;
+  const int64_t toff = b * (int64_t)(N * W) + t * W + cc;
+  C* base = reinterpret_cast<C*>(c.A) + o * c.outer_stride + toff;
   const C* tw = reinterpret_cast<const C*>(c.tw);
-  cp2 x[E];
-  {
-    const float4* sp = reinterpret_cast<const float4*>(stage_st + s * SLW) + t * 2 + p;
+  C* sm = smem + s * SLT + cc;
+  C x[E];
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const float4 v = sp[j * TPL * 2];
-      x[j] = {f2(v.x, v.z), f2(v.y, v.w)};
-    }
-  }
-  const int64_t toff = b * (int64_t)TILE + (int64_t)t * W + 2 * p;
+  for (int j = 0; j < E; ++j) x[j] = base[j * TPL * W];
+  fft_line<float, N, E, 1, false>(x, t, sm, W, tw);
   const int64_t pb = (o % c.comps) * c.prop_cstride + toff;
-  float4 pre[E];
 #pragma unroll
-  for (int j = 0; j < E; ++j)
-    pre[j] = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const C*>(c.prop) + pb +
-                                                   (int64_t)j * TPL * W));
-  __syncthreads();  // every thread has read the stage
-  float4* sA = reinterpret_cast<float4*>(stage_st + s * SLW) + p;
-  float4* sB = reinterpret_cast<float4*>(xch + s * SLW) + p;
-  pfft_db<N, E, 1, false, 0, 1, false>(x, t, sA, sB, 2, tw);
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    const float2 pr = f2(pre[j].x, pre[j].z), pi = f2(pre[j].y, pre[j].w);
-    x[j] = {fnma2(x[j].im, pi, mul2(x[j].re, pr)), fma2(x[j].re, pi, mul2(x[j].im, pr))};
-  }
-  pfft_db<N, E, 1, true, NEX % 2, 1, false>(x, t, sA, sB, 2, tw);
-  if (threadIdx.x == 0) refill();
+  for (int j = 0; j < E; ++j) x[j] = mul_prop<float, false>(x[j], c.prop, pb + j * TPL * W);
+  fft_line<float, N, E, 1, true>(x, t, sm, W, tw);
   if (act) {
-    float4* gp = reinterpret_cast<float4*>(reinterpret_cast<C*>(c.A) + o * c.outer_stride + toff);
 #pragma unroll
-    for (int j = 0; j < E; ++j)
-      gp[(int64_t)j * TPL * 2] = make_float4(x[j].re.x, x[j].im.x, x[j].re.y, x[j].im.y);
+    for (int j = 0; j < E; ++j) base[j * TPL * W] = x[j];
   }
 }
 
-// (a template so that only the translation unit that launches it compiles it)
+// two CTAs per SM (64 registers, 2 x 69.6 KB), as k_cols_blk at 2048 points
 template <int UNUSED = 0>
-__global__ void __launch_bounds__(256, 1) k_cols_pair_multi(const __grid_constant__ ColMulti m) {
-  using C = float2;
+__global__ void __launch_bounds__(kMultiTileThreads, 2) k_cols_tile_multi(
+    const __grid_constant__ ColMulti m) {
   extern __shared__ __align__(128) unsigned char smraw[];
-  C* stage = reinterpret_cast<C*>(smraw);
-  C* xch = stage + kColStages * kMultiColTile;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + kMultiColTile);
-  if (!smem_base_aligned(stage)) {
-    if (threadIdx.x == 0 && m.nplans > 0) atomicExch(m.p[0].c.status, DEV_SMEM_MISALIGNED);
-    return;
-  }
-  // bulk copies of item `item` (its tiles side by side) into stage st (thread 0)
-  auto issue = [&](int st, unsigned item) {
-    const int k = multi_plan_of(item, m);
-    const ColArgs& c = m.p[k].c;
-    const int N = 1 << m.p[k].log2n, SUB = 2048 / N;
-    const int SLW = kMultiColTile / SUB;
-    const unsigned tile_bytes = (unsigned)N * BlkW<float>::W * (unsigned)sizeof(C);
-    const int64_t nouter = c.nblocks / c.ncb;
-    const int64_t t0 = (int64_t)(item - m.p[k].item0) * SUB;
-    int nt = 0;
-    for (int s = 0; s < SUB; ++s) nt += (t0 + s < c.nblocks);
-    mbar_arrive_expect_tx(&bar[st], nt * tile_bytes);
-    for (int s = 0; s < SUB; ++s) {
-      const int64_t ti = t0 + s;
-      if (ti >= c.nblocks) break;
-      const C* src = reinterpret_cast<const C*>(c.A) + (ti % nouter) * c.outer_stride +
-                     (ti / nouter) * (int64_t)N * BlkW<float>::W;
-      bulk_load(stage + st * kMultiColTile + s * SLW, src, tile_bytes, &bar[st]);
-    }
-  };
-  if (threadIdx.x == 0) {
-    for (int st = 0; st < kColStages; ++st) mbar_init(&bar[st], 1);
-    mbar_init_fence();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int st = 0; st < kColStages; ++st) {
-      const unsigned i = blockIdx.x + (unsigned)st * gridDim.x;
-      if (i < m.items) issue(st, i);
-    }
-  int it = 0;
-  for (unsigned item = blockIdx.x; item < m.items; item += gridDim.x, ++it) {
-    const int st = it % kColStages;
-    const unsigned par = (it / kColStages) & 1;
-    const int k = multi_plan_of(item, m);
-    const ColArgs& c = m.p[k].c;
-    const bool ok = mbar_wait_bounded(&bar[st], par);
-    if (!__syncthreads_and(ok)) {
-      if (threadIdx.x == 0) {
-        atomicExch(c.status, DEV_WAIT_TIMEOUT);
-        mbar_wait_bounded(&bar[st], par);
-        if (item + gridDim.x < m.items)
-          mbar_wait_bounded(&bar[st ^ 1], ((it + 1) / kColStages) & 1);
-      }
-      return;
-    }
-    const unsigned g = item - m.p[k].item0;
-    const unsigned next = item + (unsigned)kColStages * gridDim.x;
-    auto refill = [&] {
-      if (next < m.items) {
-        fence_proxy_async_smem();
-        issue(st, next);
-      }
-    };
-    C* sst = stage + st * kMultiColTile;
-    switch (m.p[k].log2n) {
-      case 8: pair_col_item<256>(c, g, sst, xch, refill); break;
-      case 9: pair_col_item<512>(c, g, sst, xch, refill); break;
-      case 10: pair_col_item<1024>(c, g, sst, xch, refill); break;
-      default: pair_col_item<2048>(c, g, sst, xch, refill); break;
-    }
+  float2* sm = reinterpret_cast<float2*>(smraw);
+  const unsigned item = blockIdx.x;
+  const int k = multi_plan_of(item, m);
+  const ColArgs& c = m.p[k].c;
+  const unsigned g = item - m.p[k].item0;
+  switch (m.p[k].log2n) {
+    case 8: tile_col_item<256>(c, g, sm); break;
+    case 9: tile_col_item<512>(c, g, sm); break;
+    case 10: tile_col_item<1024>(c, g, sm); break;
+    default: tile_col_item<2048>(c, g, sm); break;
   }
 }
 

@@ -84,28 +84,44 @@ class DDGPE(CNLSE):
         """
         simu._add_noise(A, i, noise)
 
-    def _noise_sigmas(self, noise: float) -> tuple:
+    def _noise_sigmas(self, noise: float, nf: int | None = None) -> tuple:
+        """Standard deviation of each component's noise: one value, or one per
+        field when gamma / gamma2 are per-field arrays (the reference
+        broadcasts gamma of shape (B, 1, 1) against its (NY, NX) draw)."""
         out = []
         for gam in (self.gamma, self.gamma2):
             g = np.asarray(_host(gam), dtype=np.float64).reshape(-1)
-            if g.size != 1:
-                raise NotImplementedError("add_noise with per-field gamma")
+            if nf is not None and g.size not in (1, nf):
+                raise ValueError(f"gamma with {g.size} values for {nf} fields")
             if np.iscomplexobj(self.delta_z):
                 raise NotImplementedError("add_noise with a complex delta_z")
-            out.append(float(noise * np.sqrt(g[0] / (4 * (self.delta_X * self.delta_Y)))
-                             * self.delta_z))
+            out.append(noise * np.sqrt(g / (4 * (self.delta_X * self.delta_Y))) * self.delta_z)
         return tuple(out)
 
     def _add_noise(self, A, i: int, noise: float) -> None:
         engine.require_cuda(A)
-        s0, s1 = self._noise_sigmas(noise)
         lead = self._lead_shape(tuple(A.shape))
         nf = int(np.prod(lead)) if lead else 1
+        s0, s1 = self._noise_sigmas(noise, nf)
         lib = _lib.load()
+        pix = self.NY * self.NX
+        seed = int(self.noise_seed) & (2**64 - 1)
         with torch.cuda.device(A.device):
-            _lib.check(lib.nlse_add_noise(A.data_ptr(), engine.dtype_code(A), nf,
-                                          self.NY * self.NX, s0, s1, int(self.noise_seed) & (2**64 - 1),
-                                          int(i), engine.stream_handle(A.device)), "add_noise")
+            st = engine.stream_handle(A.device)
+            if s0.size == 1 and s1.size == 1:
+                _lib.check(lib.nlse_add_noise(A.data_ptr(), engine.dtype_code(A), nf, pix,
+                                              float(s0[0]), float(s1[0]), seed, int(i), st),
+                           "add_noise")
+                return
+            # per-field scales: the same draws (counter = pixel and step) for
+            # every field, each field scaled by its own gamma
+            s0 = np.broadcast_to(s0, (nf,))
+            s1 = np.broadcast_to(s1, (nf,))
+            fbytes = 2 * pix * A.element_size()
+            for f in range(nf):
+                _lib.check(lib.nlse_add_noise(A.data_ptr() + f * fbytes, engine.dtype_code(A), 1, pix,
+                                              float(s0[f]), float(s1[f]), seed, int(i), st),
+                           "add_noise")
 
     @staticmethod
     def laser_excitation(simu, A, t, i, F_pump_r, F_pump_t, F_probe_r, F_probe_t) -> None:

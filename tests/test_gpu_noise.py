@@ -83,3 +83,23 @@ def test_ddgpe_noise_in_the_loop_graph_equals_host_loop(monkeypatch):
     b = _loop(monkeypatch, False)
     assert np.array_equal(a, b)
     assert a[-10:].min() > 0
+
+
+def test_per_field_gamma_scales_the_shared_draws():
+    """gamma of shape (B, 1, 1) (the reference broadcasts it against its one
+    (NY, NX) draw): every field gets the same draws times its own scale."""
+    d = _ddgpe()
+    B = 3
+    gam = np.array([0.5, 1.0, 2.0]).reshape(B, 1, 1) * d.gamma
+    A = torch.zeros((B, 2, 32, 32), dtype=torch.complex128, device="cuda")
+    d.gamma = gam
+    d._add_noise(A, 4, 0.1)
+    got = A.cpu().numpy()
+    d.gamma = float(gam[1, 0, 0])
+    A1 = torch.zeros((1, 2, 32, 32), dtype=torch.complex128, device="cuda")
+    d._add_noise(A1, 4, 0.1)
+    one = A1.cpu().numpy()[0]
+    for b in range(B):
+        scale = np.sqrt(gam[b, 0, 0] / gam[1, 0, 0])
+        np.testing.assert_allclose(got[b, 0], scale * one[0], rtol=1e-12, atol=0)
+        np.testing.assert_array_equal(got[b, 1], one[1])  # gamma2 is shared
