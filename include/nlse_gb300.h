@@ -67,7 +67,8 @@ typedef struct {
  *   0 dz, 1 alpha (already halved as the reference passes alpha/2),
  *   2 g_self, 3 g_cross, 4 Isat_self, 5 Isat_cross (converted units, inf for
  *   none), 6 vscale (V' = vscale * V).
- * [14], [15]: cos and sin of (omega/2)*dz for the Rabi rotation.
+ * [14], [15]: cos and sin of (omega/2)*dz for the Rabi rotation (real parts
+ * when dz is complex); [34], [35]: their imaginary parts (0 for a real dz).
  * [30]: dz of the DDGPE pump term.
  * [32], [33]: imaginary part of dz of set 0 and set 1 (imaginary-time
  * evolution with a complex delta_z, NLSE/nlse.py:505-508; else 0).

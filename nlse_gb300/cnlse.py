@@ -107,9 +107,13 @@ class CNLSE(NLSE):
                 [np.full(nf, np.real(dzs)), a2, g22, g21, is2, is1, np.full(nf, k2 / 2)], axis=1)
             P[:, 32 + s] = np.imag(dzs)
         if self.omega is not None:
-            if np.iscomplexobj(dz):
-                raise NotImplementedError("Rabi coupling with a complex delta_z")
             w = pf(_host(self.omega) / 2, "omega")
-            P[:, 14] = np.cos(w * dz)
-            P[:, 15] = np.sin(w * dz)
+            if np.iscomplexobj(dz):
+                # the reference's cp.cos / cp.sin of a complex step (kernels_gpu.py:155-156)
+                cw, sw = np.cos(w * dz), np.sin(w * dz)
+                P[:, 14], P[:, 15] = cw.real, sw.real
+                P[:, 34], P[:, 35] = cw.imag, sw.imag
+            else:
+                P[:, 14] = np.cos(w * dz)
+                P[:, 15] = np.sin(w * dz)
         return P

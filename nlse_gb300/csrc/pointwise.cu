@@ -124,9 +124,9 @@ __global__ void k_nl_point(const StepArgs a) {
       cpx<T> y0 = nl_point<T>(x0, a0, a1, p0, has_v, v0);
       cpx<T> y1 = nl_point<T>(x1, a1, a0, p1, has_v, v1);
       if (a.flags & F_RABI) {
-        const T rc = P[14], rs = P[15];
-        const cpx<T> z0 = mk<T>(rc * y0.x + rs * y1.y, rc * y0.y - rs * y1.x);
-        const cpx<T> z1 = mk<T>(rc * y1.x + rs * y0.y, rc * y1.y - rs * y0.x);
+        const T rc = P[14], rs = P[15], ric = P[34], ris = P[35];
+        const cpx<T> z0 = rabi_rot<T>(y0, y1, rc, rs, ric, ris);
+        const cpx<T> z1 = rabi_rot<T>(y1, y0, rc, rs, ric, ris);
         y0 = z0;
         y1 = z1;
       }
@@ -217,9 +217,9 @@ __global__ void k_nl_point_pad(const StepArgs a, const cpx<T>* __restrict__ X, i
       cpx<T> y0 = nl_point<T>(A[i0], c.x, c.y, p0, has_v, v0);
       cpx<T> y1 = nl_point<T>(A[i1], c.y, c.x, p1, has_v, v1);
       if (a.flags & F_RABI) {
-        const T rc = P[14], rs = P[15];
-        const cpx<T> z0 = mk<T>(rc * y0.x + rs * y1.y, rc * y0.y - rs * y1.x);
-        const cpx<T> z1 = mk<T>(rc * y1.x + rs * y0.y, rc * y1.y - rs * y0.x);
+        const T rc = P[14], rs = P[15], ric = P[34], ris = P[35];
+        const cpx<T> z0 = rabi_rot<T>(y0, y1, rc, rs, ric, ris);
+        const cpx<T> z1 = rabi_rot<T>(y1, y0, rc, rs, ric, ris);
         y0 = z0;
         y1 = z1;
       }

@@ -321,6 +321,16 @@ __device__ __forceinline__ cp2 nl_pair_point(cp2 x, const NLP2& p, bool has_v, f
   return {fnma2(x.im, ci, mul2(x.re, cr)), fma2(x.re, ci, mul2(x.im, cr))};
 }
 
+// Rabi rotation (kernels_gpu.py:142-156): y' = c y - i s yo with c, s the
+// cosine and sine of (omega/2) dz -- complex for a complex dz (ci, si their
+// imaginary parts), else the real form of the reference's real step.
+template <typename T>
+__device__ __forceinline__ cpx<T> rabi_rot(cpx<T> y, cpx<T> yo, T rc, T rs, T ci, T si) {
+  if (ci == T(0) && si == T(0)) return mk<T>(rc * y.x + rs * yo.y, rc * y.y - rs * yo.x);
+  return mk<T>(rc * y.x - ci * y.y + rs * yo.y + si * yo.x,
+               rc * y.y + ci * y.x + si * yo.y - rs * yo.x);
+}
+
 template <typename T>
 __device__ __forceinline__ T inv_n_of(const StepArgs& a) {
   if constexpr (std::is_same<T, float>::value) return a.inv_nf;
@@ -410,10 +420,12 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
   const T* asq = reinterpret_cast<const T*>(a.asq);
   const int64_t qb_s = (f * NC + comp) * a.pix + pix0;
   const int64_t qb_o = (f * NC + (1 - comp)) * a.pix + pix0;
-  T rc = T(0), rs = T(0);
+  T rc = T(0), rs = T(0), ric = T(0), ris = T(0);
   if (rabi) {
     rc = __ldg(param_block<T>(a) + f * kParamStride + 14);
     rs = __ldg(param_block<T>(a) + f * kParamStride + 15);
+    ric = __ldg(param_block<T>(a) + f * kParamStride + 34);
+    ris = __ldg(param_block<T>(a) + f * kParamStride + 35);
   }
 #pragma unroll
   for (int j = 0; j < E; ++j) {
@@ -441,7 +453,7 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
       // kernels_gpu.py:154-156: A1' = cos*A1 - i*sin*A2, A2' = cos*A2 - i*sin*A1
       const cpx<T> vo = has_v ? load_vp<T>(a.V, a.flags, vb + j * TPL, po.vs) : mk<T>(T(0), T(0));
       const cpx<T> yo = nl_point<T, two>(xo[j], ao, as, po, has_v, vo);
-      y = mk<T>(rc * y.x + rs * yo.y, rc * y.y - rs * yo.x);
+      y = rabi_rot<T>(y, yo, rc, rs, ric, ris);
     }
     x[j] = y;
   }

@@ -26,6 +26,7 @@ variant is the timed CPU baseline.
 
 from __future__ import annotations
 
+import cmath
 import math
 from typing import Callable
 
@@ -80,7 +81,10 @@ def rabi_coupling(A1, A2, dz, omega) -> None:
     cos/sin are Python floats, so they round to the field precision as the
     CuPy fused kernel's scalars do.
     """
-    cw, sw = math.cos(omega * dz), math.sin(omega * dz)
+    if isinstance(omega * dz, complex):  # a complex step: complex cos and sin
+        cw, sw = cmath.cos(omega * dz), cmath.sin(omega * dz)
+    else:
+        cw, sw = math.cos(omega * dz), math.sin(omega * dz)
     A1_old = A1.copy()
     A1[:] = cw * A1 - 1j * sw * A2
     A2[:] = cw * A2 - 1j * sw * A1_old

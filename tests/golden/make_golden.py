@@ -115,7 +115,8 @@ def _install_shims() -> None:
     def _weak(f):
         def g(x, *a, **k):
             if np.ndim(x) == 0 and not a and not k:
-                return float(f(x))
+                y = f(x)
+                return complex(y) if np.iscomplexobj(y) else float(y)
             return f(x, *a, **k)
         return g
 

@@ -17,6 +17,8 @@ Parts (each writes .npz files under tests/golden/):
   ddgpe128  the four DDGPE cases with complex128 fields and pump profiles
             -> ddgpe_c128_<branch>.npz
             (replayed by the golden tests like every other fixture).
+  imagtime  CNLSE with Rabi coupling and a complex delta_z, complex128
+            -> cnlse_c128_single_rabi_cdz.npz (+ spread/).
   maps      NLSE 2-D with n2, alpha and Isat varying over the grid -> maps_*.npz
             (golden fixtures; run before spread and short, which cover them).
   fullsize  the benchmark configurations at their stated sizes (outputs
@@ -164,6 +166,28 @@ def part_ddgpe128() -> None:
         save(HERE / f"{name}.npz", **arrays)
 
 
+def part_imagtime() -> None:
+    """CNLSE with Rabi coupling and a complex delta_z (imaginary-time
+    evolution, NLSE/nlse.py:505-508): the cnlse_c128_single_rabi inputs with
+    dz = (1 - 0.4j) 5e-5 -- the reference's rabi_coupling then takes the
+    complex cosine and sine of the step (kernels_gpu.py:155-156)
+    -> cnlse_c128_single_rabi_cdz.npz and its spread/ entry."""
+    gc, _ = _cases()
+    use_fft("scipy")
+    name = "cnlse_c128_single_rabi_cdz"
+    arrays = dict(gc.load("cnlse_c128_single_rabi"))
+    arrays["dz"] = np.array((1 - 0.4j) * 5e-5)
+    np.savez_compressed(HERE / f"{name}.npz", **{**arrays, "out": np.zeros(0)})
+    arrays["out"] = gc.run(name, "reference")
+    save(HERE / f"{name}.npz", **arrays)
+    outs = {}
+    for kind in ("numpy", "torch"):
+        use_fft(kind)
+        outs[f"out_{kind}"] = gc.run(name, "reference")
+    use_fft("scipy")
+    save(HERE / "spread" / f"{name}.npz", **outs)
+
+
 def part_maps() -> None:
     """NLSE 2-D with n2, alpha and Isat varying over the grid (the reference
     broadcasts them in nl_prop; float64 arrays make it evaluate the step in
@@ -290,7 +314,8 @@ _R = None
 
 def main() -> None:
     global _R
-    parts = [a for a in sys.argv[1:] if a in ("spread", "short", "ddgpe128", "maps", "fullsize")
+    parts = [a for a in sys.argv[1:] if a in ("spread", "short", "ddgpe128", "maps", "imagtime",
+                                              "fullsize")
              or a.startswith("fullsize:")]
     args = [a for a in sys.argv[1:] if a not in parts]
     sys.argv = [sys.argv[0]] + args
@@ -303,7 +328,7 @@ def main() -> None:
 
     gc.set_reference(_R)
     print(f"reference NLSE {_R.__version__} from {ref}")
-    for part in parts or ["maps", "spread", "short", "ddgpe128", "fullsize"]:
+    for part in parts or ["maps", "spread", "short", "ddgpe128", "imagtime", "fullsize"]:
         t = time.time()
         if part == "maps":
             part_maps()
@@ -313,6 +338,8 @@ def main() -> None:
             part_short()
         elif part == "ddgpe128":
             part_ddgpe128()
+        elif part == "imagtime":
+            part_imagtime()
         elif part.startswith("fullsize"):
             sel = part.split(":", 1)[1].split(",") if ":" in part else ("nlse2048", "cnlse1024",
                                                                         "mixed")

@@ -130,7 +130,8 @@ def run(name: str, kind: str, upcast: bool = False, steps: int | None = None):
         omega = float(f["meta"][3])
         sim = C["CNLSE"](ALPHA, 0.5, WINDOW, N2, -0.8e-9, None, 20e-3, NX=32, NY=32, Isat=ISAT,
                          omega=None if omega < 0 else omega)
-        sim.delta_z = 5e-5
+        # (a complex step: imaginary-time evolution with the Rabi rotation)
+        sim.delta_z = complex(f["dz"][()]) if "dz" in f else 5e-5
         sim.power2 = 0.05
         sim.n22 = -1.2e-9
         sim.k2 = 2 * np.pi / 795e-9

@@ -57,10 +57,32 @@ def test_nlse_1d_and_cnlse_complex_step():
     assert cases.rel_l2(got, ref) <= 1e-12
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-12), (np.complex64, 1e-5)])
+def test_rabi_coupling_with_complex_step(dtype, tol):
+    """The Rabi rotation with the complex cosine and sine of (omega/2) dz, as the
+    reference's rabi_coupling on a complex step (kernels_gpu.py:155-156)."""
+    kw = dict(NX=32, NY=32, Isat=cases.ISAT, omega=2e3)
+    p = ng.CNLSE(cases.ALPHA, 0.5, cases.WINDOW, cases.N2, -0.8e-9, None, 20e-3, **kw)
+    o = orc.OracleCNLSE(cases.ALPHA, 0.5, cases.WINDOW, cases.N2, -0.8e-9, None, 20e-3, **kw)
+    E = np.stack([cases.gaussian(p.XX, p.YY), 0.3 * cases.gaussian(p.XX, p.YY)]).astype(dtype)
+    for s in (p, o):
+        s.delta_z = (1 - 0.4j) * 5e-5
+    got = p.out_field(E, 20 * 5e-5, verbose=False)
+    ref, _ = o.out_field(E, 20 * 5e-5)
+    assert cases.rel_l2(got, ref) <= tol
+
+
 def test_complex_step_rejected_where_unsupported():
-    cn = ng.CNLSE(cases.ALPHA, 0.5, cases.WINDOW, cases.N2, -0.8e-9, None, 20e-3, NX=32, NY=32,
-                  omega=1e3)
-    cn.delta_z = -1j * 5e-5
-    E = np.stack([cases.gaussian(cn.XX, cn.YY)] * 2).astype(np.complex128)
+    """DDGPE with a complex step raises (not built)."""
+    H = 0.654
+    d = ng.DDGPE(gamma=0.07 / H, power=1.0, window=64.0, g=1e-2 / H, omega=5.07 / H, T=2.0,
+                 omega_exc=1484.44 / H, omega_cav=1482.76 / H, detuning=0.17 / H, k_z=27.0,
+                 NX=32, NY=32)
+    d.delta_z = -1j * 0.1 / 32
+    E = np.zeros((2, 32, 32), dtype=np.complex128)
+    n = 70
+    Fr = np.zeros((32, 32), dtype=np.complex128)
+    Ft = np.zeros(n, dtype=np.complex128)
     with pytest.raises(NotImplementedError):
-        cn.out_field(E, 5e-4, verbose=False)
+        d.out_field(E, 0.1, d.laser_excitation, verbose=False, callback=[lambda *a: None],
+                    callback_args=[[Fr, Ft, Fr, Ft], []])
