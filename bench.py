@@ -577,6 +577,10 @@ def mixed_batch_leg(steps, dev, rank=0, world=1, dist=None):
     from tests import cases
 
     jobs = cases.mixed_batch(MIXED_GROUPS, seed=11 + rank)
+    for sim, _ in jobs:
+        # the per-field potentials and the propagators stay on the device
+        sim.V = torch.from_numpy(sim.V).to(dev)
+        sim.propagator = torch.from_numpy(sim._build_propagator()).to(dev)
     jobs = [(sim, torch.from_numpy(E).to(dev)) for sim, E in jobs]
     nf = sum(n for n, _ in MIXED_GROUPS)
 
@@ -611,12 +615,12 @@ def mixed_batch_leg(steps, dev, rank=0, world=1, dist=None):
             "call_setup_ms": (tb - nb * loop) * 1e3,
             "fused": ngb.last_fused, "launches_per_step": 2 if ngb.last_fused else None,
             "note": "96@256^2 + 48@512^2 + 16@1024^2 + 4@2048^2 complex64, per-field power, n2 "
-                    "and potentials, device-resident; out_fields (one CUDA graph: one column "
-                    "pass and one row pass per step over every grid size when fused); "
-                    "field_steps_per_s: median of 7 calls of `steps` steps including each "
-                    "call's set-up (uploads of parameters, normalisation, first forward "
-                    "pass); loop_*: per step, from the difference between calls of "
-                    f"{3 * steps} and {steps} steps"}
+                    "and potentials, fields and potentials device-resident; out_fields (one "
+                    "CUDA graph: one column pass and one row pass per step over every grid "
+                    "size when fused); field_steps_per_s: median of 7 calls of `steps` steps "
+                    "including each call's set-up (parameter blocks, normalisation, graph "
+                    "update, first forward pass); loop_*: per step, from the difference "
+                    f"between calls of {3 * steps} and {steps} steps"}
 
 
 def mixed_only(args):

@@ -145,6 +145,7 @@ struct nlse_plan_s {
   int64_t pix = 0;  // pixels of one component of one field
   cudaStream_t cap = nullptr;  // private stream used only for graph capture
   cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t glaunched = nullptr;  // recorded after each launch of gexec
   GraphKey gkey;
   bool gvalid = false;
   // 2-D fast path: spectral scratch in the blocked layout and the
@@ -748,6 +749,7 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
 int nlse_plan_destroy(nlse_plan p) {
   if (!p) return NLSE_OK;
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->glaunched) cudaEventDestroy(p->glaunched);
   if (p->cap) cudaStreamDestroy(p->cap);
   if (p->S) cudaFree(p->S);
   if (p->prop_blk) cudaFree(p->prop_blk);
@@ -838,6 +840,7 @@ struct nlse_group_s {
   std::vector<cudaEvent_t> ev;
   cudaEvent_t fork = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t launched = nullptr;  // recorded after each launch of gexec
   std::vector<uint8_t> key;  // serialized arguments of the captured graph
   int fused = 0;             // the captured graph runs two launches per step for the batch
 };
@@ -850,6 +853,7 @@ int nlse_group_create(nlse_group* out) {
   auto* g = new nlse_group_s();
   cudaError_t e = cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->launched, cudaEventDisableTiming);
   // kernel attributes of the one-launch-per-pass kernels (outside any capture)
   if (e == cudaSuccess) e = launch_rows_multi(0, 0, nullptr, nullptr, nullptr, 0, nullptr, true);
   if (e == cudaSuccess) e = launch_cols_tile_multi(0, nullptr, nullptr, nullptr, true);
@@ -867,10 +871,38 @@ int nlse_group_destroy(nlse_group g) {
   for (auto st : g->branch) cudaStreamDestroy(st);
   for (auto ev : g->ev) cudaEventDestroy(ev);
   if (g->fork) cudaEventDestroy(g->fork);
+  if (g->launched) cudaEventDestroy(g->launched);
   if (g->cap) cudaStreamDestroy(g->cap);
   delete g;
   return NLSE_OK;
 }
+
+}  // extern "C"
+
+namespace {
+// Make g's executable graph run `graph` (consumed): update the existing one in
+// place when the topology is the same (a new call with new buffers or
+// parameters), else instantiate anew.
+cudaError_t group_exec_refresh(nlse_group_s* g, cudaGraph_t graph) {
+  if (g->gexec) {
+    // the previous launch of the executable graph has finished before it changes
+    cudaEventSynchronize(g->launched);
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(g->gexec, graph, &info) == cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cudaSuccess;
+    }
+    cudaGetLastError();
+    cudaGraphExecDestroy(g->gexec);
+    g->gexec = nullptr;
+  }
+  const cudaError_t e = cudaGraphInstantiate(&g->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  return e;
+}
+}  // namespace
+
+extern "C" {
 
 int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* const* fields,
                          const nlse_operator* ops, const int64_t* nsteps, void* stream) {
@@ -910,12 +942,7 @@ int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* 
       if (rc != NLSE_OK) return rc;
       return cuda_fail(e2, "group capture");
     }
-    if (g->gexec) {
-      cudaGraphExecDestroy(g->gexec);
-      g->gexec = nullptr;
-    }
-    const cudaError_t e = cudaGraphInstantiate(&g->gexec, graph, 0);
-    cudaGraphDestroy(graph);
+    const cudaError_t e = group_exec_refresh(g, graph);
     if (e != cudaSuccess) return cuda_fail(e, "group graph instantiate");
     g->key = key;
   }
@@ -946,16 +973,12 @@ int nlse_group_propagate(nlse_group g, int32_t n, const nlse_plan* plans, void* 
       if (rc != NLSE_OK) return rc;
       return cuda_fail(e != cudaSuccess ? e : e2, "group capture");
     }
-    if (g->gexec) {
-      cudaGraphExecDestroy(g->gexec);
-      g->gexec = nullptr;
-    }
-    e = cudaGraphInstantiate(&g->gexec, graph, 0);
-    cudaGraphDestroy(graph);
+    e = group_exec_refresh(g, graph);
     if (e != cudaSuccess) return cuda_fail(e, "group graph instantiate");
     g->key = key;
   }
   NLSE_CUDA(cudaGraphLaunch(g->gexec, s), "group graph launch");
+  NLSE_CUDA(cudaEventRecord(g->launched, s), "group graph launch");
   return NLSE_OK;
 }
 
@@ -1009,6 +1032,8 @@ int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps
     if (e != cudaSuccess) return cuda_fail(e, "end capture");
     bool updated = false;
     if (p->gexec) {
+      // the previous launch of the executable graph has finished before it changes
+      if (p->glaunched) cudaEventSynchronize(p->glaunched);
       cudaGraphExecUpdateResultInfo info;
       if (cudaGraphExecUpdate(p->gexec, g, &info) == cudaSuccess) updated = true;
       else {
@@ -1030,6 +1055,9 @@ int nlse_propagate(nlse_plan p, void* A, const nlse_operator* op, int64_t nsteps
     p->gvalid = true;
   }
   NLSE_CUDA(cudaGraphLaunch(p->gexec, s), "graph launch");
+  if (!p->glaunched)
+    NLSE_CUDA(cudaEventCreateWithFlags(&p->glaunched, cudaEventDisableTiming), "graph launch");
+  NLSE_CUDA(cudaEventRecord(p->glaunched, s), "graph launch");
   return NLSE_OK;
 }
 
