@@ -201,8 +201,9 @@ int nlse_plan_get_kernels(nlse_plan plan, int32_t* rows_tma, int32_t* cols_tma,
  * the chosen variant cannot serve (two components, Rabi or pump terms, a
  * complex128 propagator, an external |A|^2) runs the TMA variant instead.
  * get returns the current choice and bit masks of the available variants
- * (bit v set: variant code v).  The plan's default is NLSE_ROWS_DEEP and
- * NLSE_COLS_PAIR where available, else the TMA variants.  No reference counterpart (the
+ * (bit v set: variant code v).  The plan's default is NLSE_ROWS_TMA (where
+ * the tensor map is available, else NLSE_ROWS_LINE) and, for one-component
+ * complex64 fields, NLSE_COLS_TILE (else NLSE_COLS_TMA where available).  No reference counterpart (the
  * reference's VkFFTApp(tune=True) tunes its FFT plan, NLSE/nlse.py:216);
  * nlse_gb300.autotune searches these. */
 #define NLSE_ROWS_LINE 0

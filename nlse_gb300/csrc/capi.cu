@@ -726,12 +726,11 @@ int nlse_plan_create(nlse_plan* out, const nlse_desc* desc) {
     if (p->cols_tma_ok) p->cols_avail |= 1u << NLSE_COLS_TMA;
     if (p->cols_tma_ok && pair && p->lg[0] >= 6 && p->lg[0] <= 11)
       p->cols_avail |= (1u << NLSE_COLS_PAIR) | (1u << NLSE_COLS_PAIR8) | (1u << NLSE_COLS_DEEP);
-    p->rows_var = (p->rows_avail >> NLSE_ROWS_DEEP & 1) ? NLSE_ROWS_DEEP
-                  : p->rows_tma                          ? NLSE_ROWS_TMA
-                                                         : NLSE_ROWS_LINE;
-    p->cols_var = (p->cols_avail >> NLSE_COLS_PAIR & 1) ? NLSE_COLS_PAIR
-                  : p->cols_tma                          ? NLSE_COLS_TMA
-                                                         : NLSE_COLS_TILE;
+    p->rows_var = p->rows_tma ? NLSE_ROWS_TMA : NLSE_ROWS_LINE;
+    // complex64 one-component plans: the tile column pass (fastest measured on
+    // the 2048^2 batch); others keep the TMA ring where it fits
+    if (d.dtype == NLSE_C64 && d.comps == 1) p->cols_tma = false;
+    p->cols_var = p->cols_tma ? NLSE_COLS_TMA : NLSE_COLS_TILE;
   }
   if (rc == NLSE_OK && p->fft_ok) rc = prepare_kernels(p);
   if (rc == NLSE_OK) {

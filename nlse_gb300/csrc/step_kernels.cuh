@@ -712,6 +712,9 @@ __global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
   for (unsigned g = blockIdx.x; g < ngroups; g += gridDim.x, ++it) {
     const int st = it & 1;  // kRowStages == 2
     const unsigned par = (it >> 1) & 1;
+    // the previous group's row stores have read the buffer this group writes
+    // as its second exchange buffer and refills
+    if (MODE == ROW_INV_NL_FWD && threadIdx.x == 0) bulk_wait_read_all();
     const bool ok = mbar_wait_bounded(&bar[st], par);
     if (!__syncthreads_and(ok)) {
       // give up: record it, let the copy in flight land (bounded), leave
@@ -763,12 +766,29 @@ __global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
       fft_line_hook<T, N, E, false, true, NEX == 1>(x, t, sA, 1, tw, [&] {
         if (threadIdx.x == 0) prefetch(st ^ 1, g + gridDim.x);
       });
-      if (act) {
-        C* dst =
-            reinterpret_cast<C*>(a.S) + slab + ((t / W) * a.lines_per_comp + m) * W + (t % W);
-        const int64_t dstr = (int64_t)TPL * a.lines_per_comp;
+      // the group's rows leave through A in natural order (a row of the
+      // blocked layout is its runs of W elements back to back: one
+      // tensor-map box) and tensor-map stores issued by thread 0, instead of
+      // 8/16-byte stores per thread; the loop's next turn waits for the
+      // stores' reads before A is written again
+      __syncthreads();  // every exchange read of A is complete
 #pragma unroll
-        for (int j = 0; j < E; ++j) dst[j * dstr] = x[j];
+      for (int j = 0; j < E; ++j) sA[t + j * TPL] = x[j];
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned q0 = g * LPC;
+        const unsigned nl = nq - q0 < (unsigned)LPC ? nq - q0 : (unsigned)LPC;
+        for (unsigned l = 0; l < nl; ++l) {
+          const unsigned fl = q_f(q0 + l), yl = q_y(q0 + l);
+#pragma unroll
+          for (int cc = 0; cc < NC; ++cc)
+#pragma unroll
+            for (int bx = 0; bx < NBOX; ++bx)
+              tensor_store_4d(&tmS, 0, (int)yl, bx * BOXB, (int)(fl * NC + cc),
+                              buf(st, (int)l, cc) + bx * BOXB * W);
+        }
+        bulk_commit_group();
       }
     } else {
       __syncthreads();  // B is no longer read
@@ -780,6 +800,7 @@ __global__ void __launch_bounds__(RowTma<T, N, NC>::THREADS) k_rows_tma(
       }
     }
   }
+  if (MODE == ROW_INV_NL_FWD && threadIdx.x == 0) bulk_wait_all();
 }
 
 // ---- column kernels -------------------------------------------------------
