@@ -38,11 +38,12 @@ extern "C" {
 #define NLSE_FNO_PART_PROJ 66     /* per-row partials of the projection: dWp [32][2], dbp [2] */
 #define NLSE_FNO_PART_LIFT 192    /* per-row partials of the lift (see nlse_fno_lift_bwd) */
 
-/* h0 = bf16(lift(xin, xs)) and the first row analysis T.
+/* h0 = bf16(lift(xin, xs)) and the first row analysis T (on tensor cores:
+ * BF16 cos/sin over quarter rows, exact quarter-turn rotations, FP32 sums).
  * xin [nb][256][256][3] float (Re E0, Im E0, V); xs [nb][2] float;
  * wl [5][32], bl [32] float. */
 int nlse_fno_lift_rows(int64_t nb, const float* xin, const float* xs, const float* wl,
-                       const float* bl, void* h0, void* T, void* stream);
+                       const float* bl, void* h0, void* T, int32_t* status, void* stream);
 
 /* Column transforms of T keeping the retained ky, times `scale`: the BF16
  * mixing operand Xc and (optional) Hs [mode][field][32] complex64, holding the
@@ -59,8 +60,10 @@ int nlse_fno_mix(int64_t nb, const void* Xc, const void* wbig, void* Y, int32_t*
 /* Zero-filled inverse column transforms of Y to the row half spectra U. */
 int nlse_fno_cols_synthesis(int64_t nb, const void* Y, void* U, void* stream);
 
-/* One layer's row pass: s = synthesis of U, z = h . Wc + s + bias (1 x 1
- * convolution on tensor cores), hn = bf16(GELU(z)) if act else bf16(z); stores
+/* One layer's row pass: s = row synthesis of U, z = h . Wc + s + bias (the
+ * 1 x 1 convolution and the synthesis both on tensor cores, the synthesis with
+ * BF16 cos/sin and bf16(U / 256^2), FP32 sums; Tn's analysis as in
+ * nlse_fno_lift_rows), hn = bf16(GELU(z)) if act else bf16(z); stores
  * z (optional), hn (optional) and the next layer's row analysis Tn (optional);
  * with out != NULL also the projection out = hn . wp + bp ([nb][256][256]
  * complex64).  wconv: nlse_fno_pack_conv's forward operand. */

@@ -149,7 +149,7 @@ SIGNATURES = [
     (name, ct.c_int, [{"p": ct.c_void_p, "l": ct.c_int64, "i": ct.c_int32, "f": ct.c_float}[c]
                       for c in sig])
     for name, sig in [
-        ("nlse_fno_lift_rows", "lppppppp"),
+        ("nlse_fno_lift_rows", "lpppppppp"),
         ("nlse_fno_cols_analysis", "lpfippp"),
         ("nlse_fno_mix", "lppppp"),
         ("nlse_fno_cols_synthesis", "lppp"),

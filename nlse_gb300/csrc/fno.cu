@@ -6,6 +6,8 @@
 //   h0      = bf16(lift(x))                      x: Re E0, Im E0, V + 2 scalars
 //   z_l     = h_l . bf16(Wc_l) + s_l + b_l       1 x 1 convolution on tensor cores
 //   s_l     = (1/N^2) Re( sum_{k in R} S_l(k) exp(+2 pi i k.x / N) )
+//             (its row stage as a BF16 contraction: bf16(cos), bf16(sin) and
+//             the row spectra as bf16(U / N^2), FP32 sums)
 //   S_l(k)  = bf16(H_l(k)) . bf16(W_l(k))        per-mode 32 x 32 complex mixing
 //   H_l(k)  = sum_x h_l(x) exp(-2 pi i k.x / N)  truncated transform
 //   h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)   GELU in its tanh form
@@ -22,7 +24,9 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "fft_core.cuh"
 #include "internal.h"
@@ -45,7 +49,6 @@ constexpr int XTILE = TILE_M * XK;  // BF16 elements per mixing A tile
 constexpr int WBIG = XK * XK;       // real 64 x 64 form of one mode's complex weights
 constexpr int WCONV = C * C;
 constexpr int PS = 17;              // pair stride of the [pixel][channel pair] buffers
-constexpr float kSynFwd = 1.0f / (N * N);
 constexpr size_t kPairBuf =
     (16 * SL > N * PS ? 16 * SL : N * PS) * sizeof(float2);  // shared by xl and the pairs
 
@@ -89,6 +92,29 @@ __device__ __forceinline__ void load_bf16x32(const __nv_bfloat16* src, float (&v
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __bfloat162float(b[i]);
 }
+
+// 32 floats as 16 packed BF16 pairs (round to nearest even), element 2i in the
+// low half of word i: the memory order of 32 consecutive BF16 values
+struct Bf16x32 {
+  uint4 q[4];
+};
+__device__ __forceinline__ Bf16x32 pack_bf16x32(const float (&v)[32]) {
+  Bf16x32 r;
+  uint32_t* w = reinterpret_cast<uint32_t*>(r.q);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    w[i] = *reinterpret_cast<const uint32_t*>(&b);
+  }
+  return r;
+}
+__device__ __forceinline__ void store_packed(__nv_bfloat16* dst, const Bf16x32& b) {
+  uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) d[i] = b.q[i];
+}
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
 // ---- row transforms (one CTA of 256 threads per image row) ----------------
 // The exchange lines xl (16 x SL) and the pair buffer [pixel][channel pair]
@@ -151,35 +177,6 @@ __device__ void row_synthesis(const float2* __restrict__ U, float scale, float2*
   __syncthreads();  // ss may share storage with the exchange lines
 #pragma unroll
   for (int e = 0; e < E; ++e) ss[(t + TPL * e) * PS + j] = make_float2(scale * x[e].x, scale * x[e].y);
-}
-
-// ---- lift + first row analysis ---------------------------------------------
-// xin [b][y][x][3] (Re E0, Im E0, V), xs [b][2] scalars; wl [5][C], bl [C].
-__global__ void __launch_bounds__(256) k_lift_rows(const float* __restrict__ xin,
-                                                    const float* __restrict__ xs,
-                                                    const float* __restrict__ wl,
-                                                    const float* __restrict__ bl,
-                                                    __nv_bfloat16* __restrict__ h0,
-                                                    float2* __restrict__ T, const float2* tw) {
-  extern __shared__ __align__(128) unsigned char smraw[];
-  float2* hs = reinterpret_cast<float2*>(smraw);
-  float2* xl = hs;
-  const int64_t row = blockIdx.x;
-  const int64_t b = row / N;
-  const int p = threadIdx.x;
-  const float* xi = xin + (row * N + p) * 3;
-  const float a0 = xi[0], a1 = xi[1], a2 = xi[2];
-  const float s0 = xs[2 * b], s1 = xs[2 * b + 1];
-  float v[32];
-#pragma unroll
-  for (int o = 0; o < C; ++o)
-    v[o] = bf16r(bl[o] + a0 * wl[o] + a1 * wl[C + o] + a2 * wl[2 * C + o] + s0 * wl[3 * C + o] +
-                 s1 * wl[4 * C + o]);
-  store_bf16x32(h0 + (row * N + p) * C, v);
-#pragma unroll
-  for (int jj = 0; jj < C / 2; ++jj) hs[p * PS + jj] = make_float2(v[2 * jj], v[2 * jj + 1]);
-  __syncthreads();
-  row_analysis(hs, xl, tw, T + row * ROWC);
 }
 
 // ---- column transforms -----------------------------------------------------
@@ -331,11 +328,127 @@ __global__ void __launch_bounds__(128) k_mix(const __nv_bfloat16* __restrict__ X
   tc_end(&st, tbase, 64);
 }
 
+// ---- row analysis and synthesis as tensor-core contractions -----------------
+// Synthesis, accumulated onto the 1 x 1 convolution: s[x][c] = sum_K Bs[x][K]
+// Us[c][K] with the BF16 basis Bs[x][kx] = cos(2 pi kx x / N), Bs[x][KX + kx] =
+// -sin(2 pi kx x / N) (256 pixel rows, two 128-row canonical tiles) and
+// Us[c][kx] = bf16(Re U(kx) / N^2), Us[c][KX + kx] = bf16(Im U(kx) / N^2)
+// (1/N^2 is a power of two: the scaling is exact).
+// Analysis over quarter rows x = 64 q + x': D[(q, c)][K] = sum_x' h[64 q + x'][c]
+// Ba[K][x'] with Ba[kx][x'] = cos(2 pi kx x' / N), Ba[KX + kx][x'] =
+// -sin(2 pi kx x' / N) (M = 4 quarters x 32 channels = 128, N = 64, K = 64; the
+// activations staged MN-major), then H_c(kx) = sum_q (-i)^(kx q) D_q: exact
+// quarter-turn rotations of the partial sums.  FP32 accumulation throughout.
+constexpr int KS = 2 * KX;           // contraction width: [Re | Im] of the kept kx
+constexpr int QW = N / 4;            // quarter-row width
+constexpr int kBasisSyn = N * KS;    // elements of Bs
+constexpr int kBasisAna = KS * QW;   // elements of Ba
+constexpr float kUScale = 1.0f / (N * N);
+constexpr size_t kStageBytes = (size_t)N * C * 2;            // one row of BF16 activations
+constexpr size_t kQuartBytes = (size_t)4 * 2 * KX * C * 4;   // D_q read back from TMEM
+constexpr uint32_t kStageKStride = 16 * 128;                 // 8 x' of all 16 (q, c/8) groups
+
+struct TcState2 {
+  uint64_t bar[2];  // [0]: convolution + synthesis, [1]: analysis
+  uint32_t taddr;
+};
+
+__device__ __forceinline__ void tc2_begin(TcState2* st, uint32_t ncols) {
+  if ((threadIdx.x >> 5) == 0) tmem_alloc(&st->taddr, ncols);
+  if (threadIdx.x == 0) {
+    mbar_init(&st->bar[0], 1);
+    mbar_init(&st->bar[1], 1);
+    mbar_init_fence();
+  }
+}
+
+// Shared-memory operands written by generic stores -> tensor core; TMEM
+// address to every thread.
+__device__ __forceinline__ uint32_t tc2_ready(TcState2* st) {
+  fence_proxy_async_smem();
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  return st->taddr;
+}
+
+__device__ __forceinline__ void tc2_end(TcState2* st, uint32_t ncols) {
+  tc_fence_before_sync();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tmem_dealloc(st->taddr, ncols);
+}
+
+// Bounded wait for phase `par` of st->bar[i] by every thread; on a timeout the
+// status word records it and thread 0 waits (bounded) once more so that no MMA
+// is in flight when tensor memory is released.
+__device__ __forceinline__ bool tc2_wait(TcState2* st, int i, unsigned par, int* status) {
+  const bool ok = __syncthreads_and(mbar_wait_bounded(&st->bar[i], par));
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(status, DEV_WAIT_TIMEOUT);
+    mbar_wait_bounded(&st->bar[i], par);
+  }
+  tc_fence_after_sync();
+  return ok;
+}
+
+// Pixel p's 32 BF16 activations into the MN-major analysis operand: core
+// matrix (x'/8, q*4 + c/8) of 8 x' rows x 8 channels at
+// (x'/8) * kStageKStride + (q*4 + c/8) * 128 bytes.
+__device__ __forceinline__ void stage_analysis(unsigned char* stage, int p, const Bf16x32& hb) {
+  const int q = p / QW, xq = p % QW;
+#pragma unroll
+  for (int c8 = 0; c8 < 4; ++c8)
+    *reinterpret_cast<uint4*>(stage + (xq >> 3) * kStageKStride + (q * 4 + c8) * 128 + (xq & 7) * 16) =
+        hb.q[c8];
+}
+
+// One thread: the four K = 16 analysis MMAs into TMEM columns [col, col + 64)
+// (completion through the caller's next commit).
+__device__ __forceinline__ void issue_analysis_async(uint32_t dcol, const unsigned char* stage,
+                                                     const __nv_bfloat16* sBa) {
+  const uint32_t idesc = umma_idesc_bf16(TILE_M, KS) | (1u << 15);  // A MN-major
+  const uint32_t s0 = smem_addr(stage), b0 = smem_addr(sBa);
+#pragma unroll
+  for (int kk = 0; kk < QW / 16; ++kk)
+    umma_bf16(dcol, umma_desc(s0 + kk * 2 * kStageKStride, kStageKStride, 128),
+              umma_desc(b0 + kk * 256, kUmmaLbo, umma_sbo(QW)), idesc, kk);
+}
+
+// D_q from TMEM (warp w: quarter w % 4, columns (w / 4) * 32: Re or Im part)
+// into quart [q][part][kx][c]; after a barrier every thread combines four
+// (kx, c) outputs H = sum_q (-i)^(kx q) D_q into out[kx][c].
+__device__ __forceinline__ void analysis_out(uint32_t dcol, float* quart, float2* out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float v[32];
+  tmem_ld32(tmem_lane_addr(dcol, warp, (warp >> 2) * 32), v);
+  float* dq = quart + ((warp & 3) * 2 + (warp >> 2)) * KX * C + lane;
+#pragma unroll
+  for (int kx = 0; kx < KX; ++kx) dq[kx * C] = v[kx];
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ROWC / 256; ++r) {
+    const int i = threadIdx.x + 256 * r, kx = i >> 5;
+    float hr = 0.f, hi = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // (a + i b) (-i)^m: m odd swaps the parts; m = 2, 3 negate the real
+      // part, m = 1, 2 the imaginary part
+      const float a = quart[(q * 2) * KX * C + i], b = quart[(q * 2 + 1) * KX * C + i];
+      const int m = (kx * q) & 3;
+      const float x = (m & 1) ? b : a, y = (m & 1) ? a : b;
+      hr += (m & 2) ? -x : x;
+      hi += ((m + 1) & 2) ? -y : y;
+    }
+    out[i] = make_float2(hr, hi);
+  }
+}
+
 // ---- layer epilogue rows: synthesis + 1x1 conv + bias + GELU [+ next analysis | projection]
 struct LayerArgs {
   const float2* U;
   const __nv_bfloat16* h;
   const __nv_bfloat16* wpack;  // 32 x 32 canonical, B[o][c] = Wc[c][o]
+  const __nv_bfloat16* basis;  // shared-memory image of Bs then Ba
   const float* bias;
   int act;
   __nv_bfloat16* z;  // pre-activation (optional)
@@ -344,21 +457,23 @@ struct LayerArgs {
   const float* wp;  // projection [C][2] and bias [2] (optional, with out)
   const float* bp;
   float2* out;
-  const float2* tw;
   int* status;
+  int64_t nrows;  // fields x N
 };
 
-constexpr size_t kLayerSmem = kPairBuf + (size_t)N * C * 2 + (size_t)WCONV * 2 + sizeof(TcState);
-
-__device__ __forceinline__ void stage_row_tiles(__nv_bfloat16* sA, const __nv_bfloat16* g) {
-  // a 256 x 32 BF16 row block as two 128 x 32 canonical tiles
-  const uint4* g4 = reinterpret_cast<const uint4*>(g);
-  uint4* s4 = reinterpret_cast<uint4*>(sA);
-  for (int i = threadIdx.x; i < N * C / 8; i += blockDim.x) {
-    const int px = i >> 2, k8 = i & 3;
-    s4[(px >> 7) * (TILE_M * C / 8) + chunk_of(px & 127, k8, C)] = g4[i];
-  }
-}
+// Shared memory of k_layer_rows (byte offsets; every operand 128-byte aligned)
+constexpr size_t kLrStage = 0;                                    // analysis operand
+constexpr size_t kLrQuart = kLrStage + kStageBytes;              // D_q read-back
+constexpr size_t kLrBasis = kLrQuart + kQuartBytes;              // Bs then Ba
+constexpr size_t kLrW = kLrBasis + (size_t)(kBasisSyn + kBasisAna) * 2;
+constexpr size_t kLrA = kLrW + (size_t)WCONV * 2;                // row tile [N][C] (two 128-row tiles)
+constexpr size_t kLrU = kLrA + kStageBytes;                      // spectral operand [C][KS]
+constexpr size_t kLrState = kLrU + (size_t)C * KS * 2;
+constexpr size_t kLayerSmem = kLrState + sizeof(TcState2);
+static_assert(kLrQuart % 128 == 0 && kLrBasis % 128 == 0 && kLrW % 128 == 0 && kLrA % 128 == 0 &&
+                  kLrU % 128 == 0 && kLrState % 8 == 0,
+              "layer row pass: shared-memory operand alignment");
+static_assert(2 * (kLayerSmem + 1024) <= 228 * 1024, "layer row pass: two CTAs per SM");
 
 __device__ __forceinline__ void issue_row_conv(uint32_t tbase, const __nv_bfloat16* sA,
                                                const __nv_bfloat16* sW, TcState* st) {
@@ -373,58 +488,237 @@ __device__ __forceinline__ void issue_row_conv(uint32_t tbase, const __nv_bfloat
   umma_commit(&st->bar);
 }
 
-__global__ void __launch_bounds__(256, 4) k_layer_rows(const LayerArgs a) {
+// One thread's share of a row's operands, loaded a row ahead: h (4 x 16 B of
+// the 16 KB row) and U (2 x 16 B of the 8 KB half spectrum).
+struct RowRegs {
+  uint4 h[4];
+  float4 u[2];
+};
+
+__device__ __forceinline__ void load_row_regs(RowRegs& r, const LayerArgs& a, int64_t row) {
+  const uint4* g4 = reinterpret_cast<const uint4*>(a.h + row * N * C);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) r.h[j] = g4[threadIdx.x + 256 * j];
+  const float4* u4 = reinterpret_cast<const float4*>(a.U + row * ROWC);
+  r.u[0] = u4[threadIdx.x];
+  r.u[1] = u4[threadIdx.x + 256];
+}
+
+// h into the two canonical 128 x 32 tiles; U as bf16(U / N^2) into the
+// [C][KS] canonical operand (row c, K = kx for Re, KX + kx for Im).
+__device__ __forceinline__ void store_row_regs(const RowRegs& r, __nv_bfloat16* sA,
+                                               __nv_bfloat16* sU) {
+  uint4* s4 = reinterpret_cast<uint4*>(sA);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = threadIdx.x + 256 * j, px = i >> 2, k8 = i & 3;
+    s4[(px >> 7) * (TILE_M * C / 8) + chunk_of(px & 127, k8, C)] = r.h[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int q = 2 * (threadIdx.x + 256 * j), kx = q >> 5, c = q & 31;  // U[kx][c], U[kx][c+1]
+    const float4 u = r.u[j];
+    sU[umma_off(c, kx, KS)] = __float2bfloat16_rn(u.x * kUScale);
+    sU[umma_off(c, KX + kx, KS)] = __float2bfloat16_rn(u.y * kUScale);
+    sU[umma_off(c + 1, kx, KS)] = __float2bfloat16_rn(u.z * kUScale);
+    sU[umma_off(c + 1, KX + kx, KS)] = __float2bfloat16_rn(u.w * kUScale);
+  }
+}
+
+// Persistent: each CTA walks rows blockIdx.x, +gridDim.x, ...  Per row one
+// round trip to the tensor core: the row's convolution + synthesis MMAs go
+// out together with the previous row's analysis MMAs, and while they run the
+// next row's operands are loaded into registers (stored once the MMAs have
+// completed).  TMEM: columns [0, 64) convolution + synthesis (two 128-pixel
+// tiles), [64, 128) analysis of the previous row.
+__global__ void __launch_bounds__(256, 2) k_layer_rows(const LayerArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
-  float2* xl = reinterpret_cast<float2*>(smraw);
-  float2* ss = xl;
-  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smraw + kPairBuf);
-  __nv_bfloat16* sW = sA + N * C;
-  TcState* st = reinterpret_cast<TcState*>(sW + WCONV);
-  const int64_t row = blockIdx.x;
+  unsigned char* stage = smraw + kLrStage;
+  float* quart = reinterpret_cast<float*>(smraw + kLrQuart);
+  __nv_bfloat16* sB = reinterpret_cast<__nv_bfloat16*>(smraw + kLrBasis);
+  __nv_bfloat16* sBa = sB + kBasisSyn;
+  __nv_bfloat16* sW = reinterpret_cast<__nv_bfloat16*>(smraw + kLrW);
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smraw + kLrA);
+  __nv_bfloat16* sU = reinterpret_cast<__nv_bfloat16*>(smraw + kLrU);
+  TcState2* st = reinterpret_cast<TcState2*>(smraw + kLrState);
+  __shared__ float sPar[C + 2 * C + 2];  // bias, then the projection wp [C][2] and bp [2]
   const int tid = threadIdx.x, warp = tid >> 5;
-  tc_begin(st, 64);
-  stage_row_tiles(sA, a.h + row * N * C);
-  if (tid < WCONV / 8)
-    reinterpret_cast<uint4*>(sW)[tid] = reinterpret_cast<const uint4*>(a.wpack)[tid];
-  const uint32_t tbase = tc_operands_ready(st);
-  if (tid == 0) issue_row_conv(tbase, sA, sW, st);
-  // spectral branch while the tensor core runs
-  row_synthesis(a.U + row * ROWC, kSynFwd, xl, a.tw, ss);
-  __syncthreads();
-  if (!tc_wait(st, a.status)) {
-    tc_end(st, tbase, 64);
-    return;
+  if ((int64_t)blockIdx.x >= a.nrows) return;
+  if (tid < C) sPar[tid] = a.bias[tid];
+  if (a.out && tid < 2 * C + 2) sPar[C + tid] = tid < 2 * C ? a.wp[tid] : a.bp[tid - 2 * C];
+  tc2_begin(st, 128);
+  {
+    const uint4* g4 = reinterpret_cast<const uint4*>(a.basis);
+    uint4* s4 = reinterpret_cast<uint4*>(sB);
+    for (int i = tid; i < (kBasisSyn + kBasisAna) / 8; i += 256) s4[i] = g4[i];
+    if (tid < WCONV / 8)
+      reinterpret_cast<uint4*>(sW)[tid] = reinterpret_cast<const uint4*>(a.wpack)[tid];
+    RowRegs r0;
+    load_row_regs(r0, a, blockIdx.x);
+    store_row_regs(r0, sA, sU);
   }
-  float v[32];
-  tmem_ld32(tmem_lane_addr(tbase, warp, (warp >> 2) * C), v);
   const int p = (warp >> 2) * TILE_M + (warp & 3) * 32 + (tid & 31);
-  float zz[32], hv[32];
+  const uint32_t idesc = umma_idesc_bf16(TILE_M, C);
+  bool ok = true;
+  int it = 0;
+  int64_t prev = -1;  // row whose analysis operand is staged
+  for (int64_t row = blockIdx.x; row < a.nrows; row += gridDim.x, ++it) {
+    // this row's operands and the previous row's staged activations (generic
+    // stores by every thread) to the tensor core
+    const uint32_t tbase = tc2_ready(st);
+    if (tid == 0) {
+      if (prev >= 0) issue_analysis_async(tbase + 2 * C, stage, sBa);
+      const uint32_t a0 = smem_addr(sA), w0 = smem_addr(sW), b0 = smem_addr(sB), u0 = smem_addr(sU);
 #pragma unroll
-  for (int o = 0; o < C; ++o) {
-    const float2 s2 = ss[p * PS + (o >> 1)];
-    zz[o] = v[o] + ((o & 1) ? s2.y : s2.x) + a.bias[o];
-    hv[o] = bf16r(a.act ? gelu(zz[o]) : zz[o]);
-  }
-  const int64_t pix = row * N + p;
-  if (a.z) store_bf16x32(a.z + pix * C, zz);
-  if (a.hn) store_bf16x32(a.hn + pix * C, hv);
-  if (a.out) {
-    float o0 = a.bp[0], o1 = a.bp[1];
+      for (int mt = 0; mt < 2; ++mt) {
 #pragma unroll
-    for (int o = 0; o < C; ++o) {
-      o0 = fmaf(hv[o], a.wp[2 * o], o0);
-      o1 = fmaf(hv[o], a.wp[2 * o + 1], o1);
+        for (int kk = 0; kk < C / 16; ++kk)
+          umma_bf16(tbase + mt * C,
+                    umma_desc(a0 + mt * TILE_M * C * 2 + kk * 256, kUmmaLbo, umma_sbo(C)),
+                    umma_desc(w0 + kk * 256, kUmmaLbo, umma_sbo(C)), idesc, kk);
+#pragma unroll
+        for (int kk = 0; kk < KS / 16; ++kk)
+          umma_bf16(tbase + mt * C,
+                    umma_desc(b0 + mt * TILE_M * KS * 2 + kk * 256, kUmmaLbo, umma_sbo(KS)),
+                    umma_desc(u0 + kk * 256, kUmmaLbo, umma_sbo(KS)), idesc, 1);
+      }
+      umma_commit(&st->bar[0]);
     }
-    a.out[pix] = make_float2(o0, o1);
-  }
-  if (a.Tn) {
-    __syncthreads();  // every thread has read ss
+    const int64_t next = row + gridDim.x;
+    RowRegs nr;
+    if (next < a.nrows) load_row_regs(nr, a, next);
+    if (!(ok = tc2_wait(st, 0, (unsigned)(it & 1), a.status))) break;
+    if (prev >= 0) analysis_out(tbase + 2 * C, quart, a.Tn + prev * ROWC);
+    float v[32];
+    tmem_ld32(tmem_lane_addr(tbase, warp, (warp >> 2) * C), v);
 #pragma unroll
-    for (int jj = 0; jj < C / 2; ++jj) ss[p * PS + jj] = make_float2(hv[2 * jj], hv[2 * jj + 1]);
-    __syncthreads();
-    row_analysis(ss, xl, a.tw, a.Tn + row * ROWC);
+    for (int o = 0; o < C; ++o) v[o] += sPar[o];  // z
+    const int64_t pix = row * N + p;
+    if (a.z) store_packed(a.z + pix * C, pack_bf16x32(v));
+    if (a.act) {
+#pragma unroll
+      for (int o = 0; o < C; ++o) v[o] = gelu(v[o]);
+    }
+    const Bf16x32 hb = pack_bf16x32(v);  // h' = bf16(GELU(z)) or bf16(z)
+    if (a.hn) store_packed(a.hn + pix * C, hb);
+    if (a.out) {
+      float o0 = sPar[C + 2 * C], o1 = sPar[C + 2 * C + 1];
+      const uint32_t* w = reinterpret_cast<const uint32_t*>(hb.q);
+#pragma unroll
+      for (int i = 0; i < C / 2; ++i) {
+        const float h0 = bf16_lo(w[i]), h1 = bf16_hi(w[i]);
+        o0 = fmaf(h0, sPar[C + 4 * i], o0);
+        o1 = fmaf(h0, sPar[C + 4 * i + 1], o1);
+        o0 = fmaf(h1, sPar[C + 4 * i + 2], o0);
+        o1 = fmaf(h1, sPar[C + 4 * i + 3], o1);
+      }
+      a.out[pix] = make_float2(o0, o1);
+    }
+    // the MMAs have completed: the operand buffers and the stage are free
+    if (next < a.nrows) store_row_regs(nr, sA, sU);
+    if (a.Tn) {
+      stage_analysis(stage, p, hb);
+      prev = row;
+    }
   }
-  tc_end(st, tbase, 64);
+  if (ok && prev >= 0) {  // the last row's analysis
+    const uint32_t tbase = tc2_ready(st);
+    if (tid == 0) {
+      issue_analysis_async(tbase + 2 * C, stage, sBa);
+      umma_commit(&st->bar[1]);
+    }
+    if (tc2_wait(st, 1, 0, a.status)) analysis_out(tbase + 2 * C, quart, a.Tn + prev * ROWC);
+  }
+  tc2_end(st, 128);
+}
+
+// ---- lift + first row analysis ---------------------------------------------
+// xin [b][y][x][3] (Re E0, Im E0, V), xs [b][2] scalars; wl [5][C], bl [C].
+// Persistent over rows; the analysis as in k_layer_rows (TMEM columns [0, 64)).
+struct LiftArgs {
+  const float* xin;
+  const float* xs;
+  const float* wl;
+  const float* bl;
+  __nv_bfloat16* h0;
+  float2* T;
+  const __nv_bfloat16* basis;  // Bs then Ba (Ba used)
+  int* status;
+  int64_t nrows;
+};
+constexpr size_t kLfStage = 0;                               // two stages
+constexpr size_t kLfQuart = kLfStage + 2 * kStageBytes;
+constexpr size_t kLfBa = kLfQuart + kQuartBytes;
+constexpr size_t kLfState = kLfBa + (size_t)kBasisAna * 2;
+constexpr size_t kLiftSmem = kLfState + sizeof(TcState2);
+
+__global__ void __launch_bounds__(256, 3) k_lift_rows(const LiftArgs a) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  float* quart = reinterpret_cast<float*>(smraw + kLfQuart);
+  __nv_bfloat16* sBa = reinterpret_cast<__nv_bfloat16*>(smraw + kLfBa);
+  TcState2* st = reinterpret_cast<TcState2*>(smraw + kLfState);
+  __shared__ float sWl[6 * C];  // wl [5][C], then bl [C]
+  const int p = threadIdx.x;
+  if ((int64_t)blockIdx.x >= a.nrows) return;
+  if (p < 5 * C) sWl[p] = a.wl[p];
+  if (p < C) sWl[5 * C + p] = a.bl[p];
+  tc2_begin(st, 128);
+  {
+    const uint4* g4 = reinterpret_cast<const uint4*>(a.basis + kBasisSyn);
+    for (int i = p; i < kBasisAna / 8; i += 256) reinterpret_cast<uint4*>(sBa)[i] = g4[i];
+  }
+  __syncthreads();  // sWl
+  // row i: stage and TMEM columns (i & 1); its MMAs run while row i - 1 is read out
+  float x0 = 0.f, x1 = 0.f, x2 = 0.f;
+  {
+    const float* xi = a.xin + ((int64_t)blockIdx.x * N + p) * 3;
+    x0 = xi[0];
+    x1 = xi[1];
+    x2 = xi[2];
+  }
+  bool ok = true;
+  int it = 0;
+  int64_t prev = -1;
+  for (int64_t row = blockIdx.x; row < a.nrows; row += gridDim.x, ++it) {
+    const int64_t b = row / N;
+    const float s0 = a.xs[2 * b], s1 = a.xs[2 * b + 1];
+    float v[32];
+#pragma unroll
+    for (int o = 0; o < C; ++o)
+      v[o] = sWl[5 * C + o] + x0 * sWl[o] + x1 * sWl[C + o] + x2 * sWl[2 * C + o] +
+             s0 * sWl[3 * C + o] + s1 * sWl[4 * C + o];
+    const Bf16x32 hb = pack_bf16x32(v);  // h0 = bf16(lift)
+    const int64_t next = row + gridDim.x;
+    if (next < a.nrows) {
+      const float* xi = a.xin + (next * N + p) * 3;
+      x0 = xi[0];
+      x1 = xi[1];
+      x2 = xi[2];
+    }
+    store_packed(a.h0 + (row * N + p) * C, hb);
+    unsigned char* stage = smraw + kLfStage + (it & 1) * kStageBytes;
+    stage_analysis(stage, p, hb);
+    const uint32_t tbase = tc2_ready(st);
+    if (p == 0) {
+      issue_analysis_async(tbase + (it & 1) * KS, stage, sBa);
+      umma_commit(&st->bar[it & 1]);
+    }
+    if (prev >= 0) {
+      const int pb = (it - 1) & 1;
+      if (!(ok = tc2_wait(st, pb, (unsigned)(((it - 1) >> 1) & 1), a.status))) {
+        if (p == 0) mbar_wait_bounded(&st->bar[it & 1], (unsigned)((it >> 1) & 1));  // row it's MMAs
+        break;
+      }
+      analysis_out(tbase + pb * KS, quart, a.T + prev * ROWC);
+    }
+    prev = row;
+  }
+  if (ok && prev >= 0) {
+    const int pb = (it - 1) & 1;
+    if (tc2_wait(st, pb, (unsigned)(((it - 1) >> 1) & 1), a.status))
+      analysis_out(st->taddr + pb * KS, quart, a.T + prev * ROWC);
+  }
+  tc2_end(st, 128);
 }
 
 // ---- backward ---------------------------------------------------------------
@@ -474,7 +768,8 @@ struct BwdArgs {
   int* status;
 };
 
-constexpr size_t kBwdSmem = kLayerSmem + (size_t)N * (C + 1) * sizeof(float);
+constexpr size_t kBwdSmem = kPairBuf + (size_t)N * C * 2 + (size_t)WCONV * 2 + sizeof(TcState) +
+                           (size_t)N * (C + 1) * sizeof(float);
 
 // dh = dhc_in + synthesis(Uin); dz = dh * GELU'(z) (or dh); dhc_out = dz Wc^T
 // on the tensor core; partial weight and bias gradients; Tg = analysis of dz.
@@ -817,11 +1112,48 @@ __global__ void __launch_bounds__(128) k_gemm_selftest(const __nv_bfloat16* __re
 }
 
 // ---- host side -------------------------------------------------------------------
-constexpr size_t kRowSmem = kPairBuf;
-constexpr size_t kLiftBwdSmem = kRowSmem + (size_t)N * 3 * sizeof(float);
+constexpr size_t kLiftBwdSmem = kPairBuf + (size_t)N * 3 * sizeof(float);
 
 std::mutex g_attr_mu;
 bool g_attr_done[64] = {};
+const __nv_bfloat16* g_basis[64] = {};
+int g_layer_ctas[64] = {};  // resident k_layer_rows CTAs of the device
+int g_lift_ctas[64] = {};   // resident k_lift_rows CTAs of the device
+
+uint16_t host_bf16_bits(double v) {
+  // double -> float (nearest) -> bfloat16 (nearest, ties to even)
+  const float f = (float)v;
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+// The contraction bases Bs then Ba in the kernels' shared-memory image
+// (caller holds g_attr_mu).
+int make_basis(int dev) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  auto val = [&](int k, int x) {
+    const int kx = k < KX ? k : k - KX;
+    const long double ang = 2.0L * pi * (long double)((kx * x) & (N - 1)) / (long double)N;
+    return k < KX ? (double)cosl(ang) : -(double)sinl(ang);
+  };
+  std::vector<uint16_t> hb((size_t)(kBasisSyn + kBasisAna));
+  for (int px = 0; px < N; ++px)
+    for (int k = 0; k < KS; ++k)
+      hb[(size_t)(px >> 7) * TILE_M * KS + umma_off(px & 127, k, KS)] = host_bf16_bits(val(k, px));
+  for (int k = 0; k < KS; ++k)
+    for (int x = 0; x < QW; ++x) hb[(size_t)kBasisSyn + umma_off(k, x, QW)] = host_bf16_bits(val(k, x));
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, hb.size() * 2);
+  if (e == cudaSuccess) e = cudaMemcpy(d, hb.data(), hb.size() * 2, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (d) cudaFree(d);
+    return shared_cuda_fail(e, "contraction bases");
+  }
+  g_basis[dev] = reinterpret_cast<const __nv_bfloat16*>(d);
+  return NLSE_OK;
+}
 
 int prepare(const float2** tw) {
   int dev = 0;
@@ -834,7 +1166,7 @@ int prepare(const float2** tw) {
   *tw = reinterpret_cast<const float2*>(t);
   std::lock_guard<std::mutex> lk(g_attr_mu);
   if (!g_attr_done[dev]) {
-    e = cudaFuncSetAttribute(k_lift_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRowSmem);
+    e = cudaFuncSetAttribute(k_lift_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLiftSmem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_layer_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)kLayerSmem);
@@ -845,6 +1177,36 @@ int prepare(const float2** tw) {
       e = cudaFuncSetAttribute(k_lift_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)kLiftBwdSmem);
     if (e != cudaSuccess) return shared_cuda_fail(e, "cudaFuncSetAttribute (FNO kernels)");
+    // persistent grids: every CTA the multiprocessors can hold (shared memory,
+    // registers and threads counted here from the kernels' attributes)
+    int nsm = 0, smem_sm = 0, smem_res = 0, regs_sm = 0, thr_sm = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&smem_res, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    if (e != cudaSuccess) return shared_cuda_fail(e, "device attributes");
+    auto resident = [&](const void* fn, size_t smem, int* out) {
+      cudaFuncAttributes fa;
+      const cudaError_t fe = cudaFuncGetAttributes(&fa, fn);
+      if (fe != cudaSuccess) return fe;
+      const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * 8;  // 8 warps, 256-register units
+      int n = (int)(smem_sm / (smem + fa.sharedSizeBytes + smem_res));
+      if (regs_cta > 0 && regs_sm / regs_cta < n) n = regs_sm / regs_cta;
+      if (thr_sm / 256 < n) n = thr_sm / 256;
+      *out = nsm * (n > 0 ? n : 1);
+      return cudaSuccess;
+    };
+    e = resident(reinterpret_cast<const void*>(k_layer_rows), kLayerSmem, &g_layer_ctas[dev]);
+    if (e == cudaSuccess)
+      e = resident(reinterpret_cast<const void*>(k_lift_rows), kLiftSmem, &g_lift_ctas[dev]);
+    if (e != cudaSuccess) return shared_cuda_fail(e, "persistent grid sizes");
+    const int brc = make_basis(dev);
+    if (brc != NLSE_OK) return brc;
     g_attr_done[dev] = true;
   }
   return NLSE_OK;
@@ -867,16 +1229,28 @@ using namespace nlse::fno;
 extern "C" {
 
 int nlse_fno_lift_rows(int64_t nb, const float* xin, const float* xs, const float* wl,
-                       const float* bl, void* h0, void* T, void* stream) {
+                       const float* bl, void* h0, void* T, int32_t* status, void* stream) {
   nlse::shared_clear_error();
-  if (bad_batch(nb) || !xin || !xs || !wl || !bl || !h0 || !T)
+  if (bad_batch(nb) || !xin || !xs || !wl || !bl || !h0 || !T || !status)
     return nlse::shared_fail(NLSE_ERR_ARG, "nlse_fno_lift_rows: bad argument");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const float2* tw;
   int rc = prepare(&tw);
   if (rc != NLSE_OK) return rc;
-  k_lift_rows<<<(unsigned)(nb * N), 256, kRowSmem, s>>>(
-      xin, xs, wl, bl, reinterpret_cast<__nv_bfloat16*>(h0), reinterpret_cast<float2*>(T), tw);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  LiftArgs a;
+  a.xin = xin;
+  a.xs = xs;
+  a.wl = wl;
+  a.bl = bl;
+  a.h0 = reinterpret_cast<__nv_bfloat16*>(h0);
+  a.T = reinterpret_cast<float2*>(T);
+  a.basis = g_basis[dev];
+  a.status = status;
+  a.nrows = nb * N;
+  const int64_t grid = a.nrows < g_lift_ctas[dev] ? a.nrows : g_lift_ctas[dev];
+  k_lift_rows<<<(unsigned)grid, 256, kLiftSmem, s>>>(a);
   return launched("nlse_fno_lift_rows");
 }
 
@@ -945,9 +1319,13 @@ int nlse_fno_layer_rows(int64_t nb, const void* U, const void* h, const void* wc
   a.wp = wp;
   a.bp = bp;
   a.out = reinterpret_cast<float2*>(out);
-  a.tw = tw;
   a.status = status;
-  k_layer_rows<<<(unsigned)(nb * N), 256, kLayerSmem, s>>>(a);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  a.basis = g_basis[dev];
+  a.nrows = nb * N;
+  const int64_t grid = a.nrows < g_layer_ctas[dev] ? a.nrows : g_layer_ctas[dev];
+  k_layer_rows<<<(unsigned)grid, 256, kLayerSmem, s>>>(a);
   return launched("nlse_fno_layer_rows");
 }
 

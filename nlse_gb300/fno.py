@@ -157,7 +157,7 @@ class FNO:
         L, P, s, nb = self.lib, self.P, stream_handle(self.dev), ws.nb
         ck = _lib.check
         ck(L.nlse_fno_lift_rows(nb, _ptr(xin), _ptr(xs), _ptr(P["wl"]), _ptr(P["bl"]),
-                                _ptr(ws.h[0]), _ptr(ws.T), s), "fno lift")
+                                _ptr(ws.h[0]), _ptr(ws.T), _ptr(self.status), s), "fno lift")
         for l in range(NL):
             last = l == NL - 1
             hin = ws.h[l] if ws.train else ws.h[l % 2]

@@ -8,9 +8,13 @@ specification it is checked against: grid N = 256, C = 32 channels, retained
 modes kx in [0, 32), ky in [0, 32) u [224, 256) (mode index iy*32 + kx).
 
     h0      = bf16(lift(x))
-    H_l     = F_R h_l                      (unnormalised DFT on the kept modes)
+    H_l     = F_R h_l                      (unnormalised DFT on the kept modes; the
+                                            row stage with BF16 cos/sin over quarter
+                                            rows, FP32 sums: analysis_rounded)
     S_l     = bf16(H_l) . bf16(W_l)         per mode, complex 32 x 32
-    s_l     = Re(ifft2(zero-filled S_l))    ((1/N^2) Re sum_k S(k) e^{+ik.x})
+    s_l     = Re(ifft2(zero-filled S_l))    ((1/N^2) Re sum_k S(k) e^{+ik.x}; the row
+                                            stage with BF16 cos/sin and BF16 row
+                                            spectra U/N^2, FP32 sums: synthesis_rounded)
     z_l     = h_l . bf16(Wc_l) + s_l + b_l
     h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)   (tanh-form GELU)
     out     = h_4 . Wp + bp                 (Re, Im)
@@ -67,6 +71,48 @@ def synthesis(S: np.ndarray) -> np.ndarray:
     return np.fft.ifft2(F, axes=(1, 2)).real
 
 
+def _basis():
+    """The BF16 row-synthesis basis: cos and sin of 2 pi kx x / N, (KX, N)."""
+    j = (np.arange(KX)[:, None] * np.arange(N)[None, :]) % N
+    ang = 2.0 * np.pi * j / N
+    return bf16(np.cos(ang)), bf16(np.sin(ang))
+
+
+def synthesis_rounded(S: np.ndarray) -> np.ndarray:
+    """synthesis() as the kernels evaluate it: the column stage exact, then
+    s(x) = sum_kx bf16(Re U(kx)/N^2) bf16(cos) - bf16(Im U(kx)/N^2) bf16(sin)
+    for each image row, U the row's half spectrum (kx < KX)."""
+    B = S.shape[0]
+    F = np.zeros((B, N, KX, S.shape[-1]), np.complex128)
+    F[:, KY_ROWS, :, :] = S.reshape(B, KY, KX, -1)
+    U = np.fft.ifft(F, axis=1) * N                      # (B, y, kx, c), unnormalised
+    ur, ui = bf16(U.real / N**2), bf16(U.imag / N**2)
+    cb, sb = _basis()
+    return np.einsum("bykc,kx->byxc", ur, cb) - np.einsum("bykc,kx->byxc", ui, sb)
+
+
+def _analysis_basis():
+    """BF16 cos and sin of 2 pi kx x' / N over a quarter row, x' < N/4: (KX, N/4)."""
+    j = (np.arange(KX)[:, None] * np.arange(N // 4)[None, :]) % N
+    ang = 2.0 * np.pi * j / N
+    return bf16(np.cos(ang)), bf16(np.sin(ang))
+
+
+def analysis_rounded(h: np.ndarray) -> np.ndarray:
+    """analysis() as the kernels evaluate it: the row stage over quarter rows
+    (x = 64 q + x') with BF16 cos/sin of 2 pi kx x' / N, the exact factor
+    (-i)^(kx q) of each quarter and FP32 sums of the BF16 activations; the
+    column stage exact."""
+    B = h.shape[0]
+    cb, sb = _analysis_basis()
+    hq = h.reshape(B, N, 4, N // 4, h.shape[-1])                 # b, y, q, x', c
+    Dq = np.einsum("byqxc,kx->byqkc", hq, cb) - 1j * np.einsum("byqxc,kx->byqkc", hq, sb)
+    rot = (-1j) ** ((np.arange(KX)[None, :] * np.arange(4)[:, None]) % 4)  # (q, kx)
+    Hrow = np.einsum("byqkc,qk->bykc", Dq, rot)                  # (B, y, kx, c)
+    F = np.fft.fft(Hrow, axis=1)
+    return F[:, KY_ROWS, :, :].reshape(B, NM, h.shape[-1])
+
+
 class Params:
     """Flat parameter vector with named views (layout of the CUDA host code)."""
 
@@ -103,10 +149,9 @@ def forward(flat: np.ndarray, xin: np.ndarray, xs: np.ndarray, exact: bool = Fal
     h = [r(lift)]
     zs, Xs = [], []
     for l in range(NL):
-        X = analysis(h[l])
-        X = X if exact else bf16c(X)
+        X = analysis(h[l]) if exact else bf16c(analysis_rounded(h[l]))
         S = np.einsum("bmc,mco->bmo", X, _cw(P[f"W{l}"], exact))
-        z = h[l] @ r(P[f"Wc{l}"]) + synthesis(S) + P[f"b{l}"]
+        z = h[l] @ r(P[f"Wc{l}"]) + (synthesis(S) if exact else synthesis_rounded(S)) + P[f"b{l}"]
         zs.append(z)
         Xs.append(X)
         h.append(r(gelu(z)) if l < NL - 1 else r(z))

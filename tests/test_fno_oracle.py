@@ -24,6 +24,30 @@ def test_synthesis_is_adjoint_of_analysis():
     assert abs(lhs - rhs) <= 1e-9 * abs(rhs)
 
 
+def test_rounded_synthesis_is_the_synthesis_to_bf16_accuracy():
+    rng = np.random.default_rng(4)
+    S = rng.normal(size=(1, fo.NM, 3)) + 1j * rng.normal(size=(1, fo.NM, 3))
+    exact, rounded = fo.synthesis(S), fo.synthesis_rounded(S)
+    rel = np.linalg.norm(rounded - exact) / np.linalg.norm(exact)
+    assert 1e-5 < rel < 1e-2, rel
+    cb, sb = fo._basis()
+    assert cb[0, 5] == 1.0 and sb[0, 5] == 0.0 and cb[8, 8] == fo.bf16(np.cos(np.pi / 2))
+
+
+def test_rounded_analysis_is_the_analysis_to_bf16_accuracy():
+    rng = np.random.default_rng(5)
+    h = fo.bf16(rng.normal(size=(1, fo.N, fo.N, 3)))
+    exact, rounded = fo.analysis(h), fo.analysis_rounded(h)
+    rel = np.linalg.norm(rounded - exact) / np.linalg.norm(exact)
+    assert 1e-5 < rel < 1e-2, rel
+    # a pure row harmonic lands on its own mode up to the basis rounding
+    x = np.arange(fo.N)
+    g = np.zeros((1, fo.N, fo.N, 1))
+    g[0, :, :, 0] = np.cos(2 * np.pi * 5 * x / fo.N)[None, :]
+    H = fo.analysis_rounded(g)[0, :, 0]
+    assert abs(H[5] - fo.N * fo.N / 2) < 1e-2 * fo.N * fo.N and np.abs(np.delete(H, 5)).max() < 2e-2 * fo.N**2
+
+
 def _problem(seed=2, B=1):
     """Seeded parameters, smooth beam-like inputs and a random target."""
     rng = np.random.default_rng(seed)

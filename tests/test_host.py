@@ -226,7 +226,7 @@ def _arg_error_cases(lib):
         ("normalize null", lambda: lib.nlse_normalize(z, z, 0, 1, 1, z, z, 1.0, z)),
         ("square_mod bad dtype", lambda: lib.nlse_square_mod(fake, fake, 9, 16, z)),
         ("fno_lift_rows empty batch",
-         lambda: lib.nlse_fno_lift_rows(0, fake, fake, fake, fake, fake, fake, z)),
+         lambda: lib.nlse_fno_lift_rows(0, fake, fake, fake, fake, fake, fake, fake, z)),
         ("fno_mix empty batch", lambda: lib.nlse_fno_mix(0, fake, fake, fake, fake, z)),
         ("fno_loss empty batch", lambda: lib.nlse_fno_loss(0, fake, fake, fake, fake, fake, z)),
         # 32769 segments of 8193 elements need 65,538 partial sums: two over the static array
