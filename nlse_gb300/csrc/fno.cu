@@ -415,32 +415,41 @@ __device__ __forceinline__ void issue_analysis_async(uint32_t dcol, const unsign
 }
 
 // D_q from TMEM (warp w: quarter w % 4, columns (w / 4) * 32: Re or Im part)
-// into quart [q][part][kx][c]; after a barrier every thread combines four
-// (kx, c) outputs H = sum_q (-i)^(kx q) D_q into out[kx][c].
+// into quart [q][part][c][kx] (rows of 32 floats, float4 j of row c at
+// position j ^ (c % 8): conflict-free 16-byte accesses); after a barrier
+// thread (c, j) combines H_c(kx) = sum_q (-i)^(kx q) D_q for kx = 4j .. 4j+3,
+// whose rotations (-i)^((kx q) % 4) = (-i)^((m q) % 4), m = kx % 4, are fixed
+// per unrolled (m, q); out[kx][c] stores coalesced over c.
 __device__ __forceinline__ void analysis_out(uint32_t dcol, float* quart, float2* out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float v[32];
-  tmem_ld32(tmem_lane_addr(dcol, warp, (warp >> 2) * 32), v);
-  float* dq = quart + ((warp & 3) * 2 + (warp >> 2)) * KX * C + lane;
+  {
+    float v[32];
+    tmem_ld32(tmem_lane_addr(dcol, warp, (warp >> 2) * 32), v);
+    float4* row = reinterpret_cast<float4*>(quart + (((warp & 3) * 2 + (warp >> 2)) * C + lane) * KX);
 #pragma unroll
-  for (int kx = 0; kx < KX; ++kx) dq[kx * C] = v[kx];
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < ROWC / 256; ++r) {
-    const int i = threadIdx.x + 256 * r, kx = i >> 5;
-    float hr = 0.f, hi = 0.f;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      // (a + i b) (-i)^m: m odd swaps the parts; m = 2, 3 negate the real
-      // part, m = 1, 2 the imaginary part
-      const float a = quart[(q * 2) * KX * C + i], b = quart[(q * 2 + 1) * KX * C + i];
-      const int m = (kx * q) & 3;
-      const float x = (m & 1) ? b : a, y = (m & 1) ? a : b;
-      hr += (m & 2) ? -x : x;
-      hi += ((m + 1) & 2) ? -y : y;
-    }
-    out[i] = make_float2(hr, hi);
+    for (int j = 0; j < KX / 4; ++j)
+      row[j ^ (lane & 7)] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
   }
+  __syncthreads();
+  const int c = lane, j = warp;  // kx = 4j .. 4j+3
+  float hr[4] = {0.f, 0.f, 0.f, 0.f}, hi[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 ar = reinterpret_cast<const float4*>(quart + ((q * 2) * C + c) * KX)[j ^ (c & 7)];
+    const float4 ai = reinterpret_cast<const float4*>(quart + ((q * 2 + 1) * C + c) * KX)[j ^ (c & 7)];
+    const float re[4] = {ar.x, ar.y, ar.z, ar.w}, im[4] = {ai.x, ai.y, ai.z, ai.w};
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      // (a + i b) (-i)^r: r odd swaps the parts; r = 2, 3 negate the real
+      // part, r = 1, 2 the imaginary part
+      const int r = (m * q) & 3;
+      const float x = (r & 1) ? im[m] : re[m], y = (r & 1) ? re[m] : im[m];
+      hr[m] += (r & 2) ? -x : x;
+      hi[m] += ((r + 1) & 2) ? -y : y;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) out[(4 * j + m) * C + c] = make_float2(hr[m], hi[m]);
 }
 
 // ---- layer epilogue rows: synthesis + 1x1 conv + bias + GELU [+ next analysis | projection]
@@ -492,37 +501,49 @@ __device__ __forceinline__ void issue_row_conv(uint32_t tbase, const __nv_bfloat
 // the 16 KB row) and U (2 x 16 B of the 8 KB half spectrum).
 struct RowRegs {
   uint4 h[4];
-  float4 u[2];
+  float2 u[4];
 };
+
+// 16-byte piece of the row's h (16 KB, 1024 pieces) handled by this thread in
+// round j: the warp's 32 pieces are its 512 contiguous bytes (8 pixels x 4
+// channel octets), lane l taking pixel l % 8 and octet l / 8, so that each
+// quarter-warp of a shared-memory store fills one 128-byte row of core matrices.
+__device__ __forceinline__ int h_piece(int j) {
+  const int l = threadIdx.x & 31;
+  return ((threadIdx.x & ~31) + 256 * j) + (l & 7) * 4 + (l >> 3);
+}
 
 __device__ __forceinline__ void load_row_regs(RowRegs& r, const LayerArgs& a, int64_t row) {
   const uint4* g4 = reinterpret_cast<const uint4*>(a.h + row * N * C);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) r.h[j] = g4[threadIdx.x + 256 * j];
-  const float4* u4 = reinterpret_cast<const float4*>(a.U + row * ROWC);
-  r.u[0] = u4[threadIdx.x];
-  r.u[1] = u4[threadIdx.x + 256];
+  for (int j = 0; j < 4; ++j) r.h[j] = g4[h_piece(j)];
+  // U[kx][c] for c = tid % 32 and kx = 4 (tid / 32) .. + 3 (coalesced over c)
+  const float2* u = a.U + row * ROWC;
+  const int c = threadIdx.x & 31, kb = threadIdx.x >> 5;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) r.u[m] = u[(4 * kb + m) * C + c];
 }
 
 // h into the two canonical 128 x 32 tiles; U as bf16(U / N^2) into the
-// [C][KS] canonical operand (row c, K = kx for Re, KX + kx for Im).
+// [C][KS] canonical operand (row c, K = kx for Re, KX + kx for Im), four
+// consecutive K per 8-byte store.
 __device__ __forceinline__ void store_row_regs(const RowRegs& r, __nv_bfloat16* sA,
                                                __nv_bfloat16* sU) {
   uint4* s4 = reinterpret_cast<uint4*>(sA);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const int i = threadIdx.x + 256 * j, px = i >> 2, k8 = i & 3;
+    const int i = h_piece(j), px = i >> 2, k8 = i & 3;
     s4[(px >> 7) * (TILE_M * C / 8) + chunk_of(px & 127, k8, C)] = r.h[j];
   }
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    const int q = 2 * (threadIdx.x + 256 * j), kx = q >> 5, c = q & 31;  // U[kx][c], U[kx][c+1]
-    const float4 u = r.u[j];
-    sU[umma_off(c, kx, KS)] = __float2bfloat16_rn(u.x * kUScale);
-    sU[umma_off(c, KX + kx, KS)] = __float2bfloat16_rn(u.y * kUScale);
-    sU[umma_off(c + 1, kx, KS)] = __float2bfloat16_rn(u.z * kUScale);
-    sU[umma_off(c + 1, KX + kx, KS)] = __float2bfloat16_rn(u.w * kUScale);
-  }
+  const int c = threadIdx.x & 31, kb = threadIdx.x >> 5;
+  const __nv_bfloat162 r01 = __floats2bfloat162_rn(r.u[0].x * kUScale, r.u[1].x * kUScale);
+  const __nv_bfloat162 r23 = __floats2bfloat162_rn(r.u[2].x * kUScale, r.u[3].x * kUScale);
+  const __nv_bfloat162 i01 = __floats2bfloat162_rn(r.u[0].y * kUScale, r.u[1].y * kUScale);
+  const __nv_bfloat162 i23 = __floats2bfloat162_rn(r.u[2].y * kUScale, r.u[3].y * kUScale);
+  *reinterpret_cast<uint2*>(sU + umma_off(c, 4 * kb, KS)) =
+      make_uint2(*reinterpret_cast<const uint32_t*>(&r01), *reinterpret_cast<const uint32_t*>(&r23));
+  *reinterpret_cast<uint2*>(sU + umma_off(c, KX + 4 * kb, KS)) =
+      make_uint2(*reinterpret_cast<const uint32_t*>(&i01), *reinterpret_cast<const uint32_t*>(&i23));
 }
 
 // Persistent: each CTA walks rows blockIdx.x, +gridDim.x, ...  Per row one
@@ -541,7 +562,7 @@ __global__ void __launch_bounds__(256, 2) k_layer_rows(const LayerArgs a) {
   __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smraw + kLrA);
   __nv_bfloat16* sU = reinterpret_cast<__nv_bfloat16*>(smraw + kLrU);
   TcState2* st = reinterpret_cast<TcState2*>(smraw + kLrState);
-  __shared__ float sPar[C + 2 * C + 2];  // bias, then the projection wp [C][2] and bp [2]
+  __shared__ __align__(16) float sPar[C + 2 * C + 2];  // bias, then the projection wp [C][2] and bp [2]
   const int tid = threadIdx.x, warp = tid >> 5;
   if ((int64_t)blockIdx.x >= a.nrows) return;
   if (tid < C) sPar[tid] = a.bias[tid];
@@ -592,7 +613,13 @@ __global__ void __launch_bounds__(256, 2) k_layer_rows(const LayerArgs a) {
     float v[32];
     tmem_ld32(tmem_lane_addr(tbase, warp, (warp >> 2) * C), v);
 #pragma unroll
-    for (int o = 0; o < C; ++o) v[o] += sPar[o];  // z
+    for (int o = 0; o < C; o += 4) {  // z
+      const float4 bq = *reinterpret_cast<const float4*>(sPar + o);
+      v[o] += bq.x;
+      v[o + 1] += bq.y;
+      v[o + 2] += bq.z;
+      v[o + 3] += bq.w;
+    }
     const int64_t pix = row * N + p;
     if (a.z) store_packed(a.z + pix * C, pack_bf16x32(v));
     if (a.act) {
@@ -607,10 +634,11 @@ __global__ void __launch_bounds__(256, 2) k_layer_rows(const LayerArgs a) {
 #pragma unroll
       for (int i = 0; i < C / 2; ++i) {
         const float h0 = bf16_lo(w[i]), h1 = bf16_hi(w[i]);
-        o0 = fmaf(h0, sPar[C + 4 * i], o0);
-        o1 = fmaf(h0, sPar[C + 4 * i + 1], o1);
-        o0 = fmaf(h1, sPar[C + 4 * i + 2], o0);
-        o1 = fmaf(h1, sPar[C + 4 * i + 3], o1);
+        const float4 wq = *reinterpret_cast<const float4*>(sPar + C + 4 * i);
+        o0 = fmaf(h0, wq.x, o0);
+        o1 = fmaf(h0, wq.y, o1);
+        o0 = fmaf(h1, wq.z, o0);
+        o1 = fmaf(h1, wq.w, o1);
       }
       a.out[pix] = make_float2(o0, o1);
     }
@@ -657,7 +685,7 @@ __global__ void __launch_bounds__(256, 3) k_lift_rows(const LiftArgs a) {
   float* quart = reinterpret_cast<float*>(smraw + kLfQuart);
   __nv_bfloat16* sBa = reinterpret_cast<__nv_bfloat16*>(smraw + kLfBa);
   TcState2* st = reinterpret_cast<TcState2*>(smraw + kLfState);
-  __shared__ float sWl[6 * C];  // wl [5][C], then bl [C]
+  __shared__ __align__(16) float sWl[6 * C];  // wl [5][C], then bl [C]
   const int p = threadIdx.x;
   if ((int64_t)blockIdx.x >= a.nrows) return;
   if (p < 5 * C) sWl[p] = a.wl[p];
@@ -684,9 +712,15 @@ __global__ void __launch_bounds__(256, 3) k_lift_rows(const LiftArgs a) {
     const float s0 = a.xs[2 * b], s1 = a.xs[2 * b + 1];
     float v[32];
 #pragma unroll
-    for (int o = 0; o < C; ++o)
-      v[o] = sWl[5 * C + o] + x0 * sWl[o] + x1 * sWl[C + o] + x2 * sWl[2 * C + o] +
-             s0 * sWl[3 * C + o] + s1 * sWl[4 * C + o];
+    for (int o = 0; o < C; o += 4) {
+      float4 w[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) w[i] = *reinterpret_cast<const float4*>(sWl + i * C + o);
+      v[o] = w[5].x + x0 * w[0].x + x1 * w[1].x + x2 * w[2].x + s0 * w[3].x + s1 * w[4].x;
+      v[o + 1] = w[5].y + x0 * w[0].y + x1 * w[1].y + x2 * w[2].y + s0 * w[3].y + s1 * w[4].y;
+      v[o + 2] = w[5].z + x0 * w[0].z + x1 * w[1].z + x2 * w[2].z + s0 * w[3].z + s1 * w[4].z;
+      v[o + 3] = w[5].w + x0 * w[0].w + x1 * w[1].w + x2 * w[2].w + s0 * w[3].w + s1 * w[4].w;
+    }
     const Bf16x32 hb = pack_bf16x32(v);  // h0 = bf16(lift)
     const int64_t next = row + gridDim.x;
     if (next < a.nrows) {
