@@ -69,7 +69,7 @@ typedef struct {
  *   none), 6 vscale (V' = vscale * V).
  * [14], [15]: cos and sin of (omega/2)*dz for the Rabi rotation (real parts
  * when dz is complex); [34], [35]: their imaginary parts (0 for a real dz).
- * [30]: dz of the DDGPE pump term.
+ * [30], [31]: real and imaginary parts of dz of the DDGPE pump term.
  * [32], [33]: imaginary part of dz of set 0 and set 1 (imaginary-time
  * evolution with a complex delta_z, NLSE/nlse.py:505-508; else 0).
  */

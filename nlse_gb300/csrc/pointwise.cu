@@ -131,17 +131,17 @@ __global__ void k_nl_point(const StepArgs a) {
         y1 = z1;
       }
       if (a.flags & (F_PUMP | F_PROBE)) {
-        const T dz = P[30];
+        const T dz = P[30], dzi = P[31];
         if (a.flags & F_PUMP) {
-          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[px],
-                             reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]);
-          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          const cpx<T> u = pump_dz<T>(cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[px],
+                                              reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]),
+                                      dz, dzi);
           y1 = mk<T>(y1.x + u.y, y1.y - u.x);
         }
         if (a.flags & F_PROBE) {
-          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.probe_r)[px],
-                             reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]);
-          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+          const cpx<T> u = pump_dz<T>(cmul<T>(reinterpret_cast<const cpx<T>*>(a.probe_r)[px],
+                                              reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]),
+                                      dz, dzi);
           y1 = mk<T>(y1.x + u.y, y1.y - u.x);
         }
       }

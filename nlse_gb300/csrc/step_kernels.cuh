@@ -331,6 +331,15 @@ __device__ __forceinline__ cpx<T> rabi_rot(cpx<T> y, cpx<T> yo, T rc, T rs, T ci
                rc * y.y + ci * y.x + si * yo.y - rs * yo.x);
 }
 
+// F * dz for the DDGPE source term A2 -= F dz i (ddgpe.py:155-156): the
+// product with a real step, or the complex product with dz = dr + i di (a
+// complex delta_z).
+template <typename T>
+__device__ __forceinline__ cpx<T> pump_dz(cpx<T> u, T dr, T di) {
+  if (di == T(0)) return mk<T>(mul_rn(u.x, dr), mul_rn(u.y, dr));
+  return cmul<T>(u, mk<T>(dr, di));
+}
+
 template <typename T>
 __device__ __forceinline__ T inv_n_of(const StepArgs& a) {
   if constexpr (std::is_same<T, float>::value) return a.inv_nf;
@@ -460,6 +469,7 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
   if (two && post && comp == 1 && (a.flags & (F_PUMP | F_PROBE))) {
     // ddgpe.py:155-156: A2 -= F_r * F_t[i] * dz * 1j  (pump, then probe)
     const T dz = __ldg(param_block<T>(a) + f * kParamStride + 30);
+    const T dzi = __ldg(param_block<T>(a) + f * kParamStride + 31);
     const cpx<T>* pr = reinterpret_cast<const cpx<T>*>(a.pump_r);
     const cpx<T>* qr = reinterpret_cast<const cpx<T>*>(a.probe_r);
     const cpx<T> ptv = (a.flags & F_PUMP) ? reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]
@@ -469,13 +479,11 @@ __device__ __forceinline__ void nl_line(cpx<T> (&x)[E], const cpx<T> (&xo)[E], c
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       if (a.flags & F_PUMP) {
-        cpx<T> u = cmul<T>(pr[pix0 + j * TPL], ptv);
-        u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+        const cpx<T> u = pump_dz<T>(cmul<T>(pr[pix0 + j * TPL], ptv), dz, dzi);
         x[j] = mk<T>(x[j].x + u.y, x[j].y - u.x);
       }
       if (a.flags & F_PROBE) {
-        cpx<T> u = cmul<T>(qr[pix0 + j * TPL], qtv);
-        u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
+        const cpx<T> u = pump_dz<T>(cmul<T>(qr[pix0 + j * TPL], qtv), dz, dzi);
         x[j] = mk<T>(x[j].x + u.y, x[j].y - u.x);
       }
     }

@@ -94,7 +94,9 @@ class DDGPE(CNLSE):
             if nf is not None and g.size not in (1, nf):
                 raise ValueError(f"gamma with {g.size} values for {nf} fields")
             if np.iscomplexobj(self.delta_z):
-                raise NotImplementedError("add_noise with a complex delta_z")
+                # the reference draws with scale=delta_z, which a complex step
+                # makes fail (ddgpe.py:114-119)
+                raise TypeError("add_noise: the noise scale delta_z must be real")
             out.append(noise * np.sqrt(g / (4 * (self.delta_X * self.delta_Y))) * self.delta_z)
         return tuple(out)
 
@@ -162,9 +164,7 @@ class DDGPE(CNLSE):
         na = len(self._last_axes)
         pf = lambda x, name: engine.per_field(_host(x), lead, na, name)  # noqa: E731
         P = np.zeros((nf, _lib.NLSE_PARAM_STRIDE), dtype=np.float64)
-        dz = self.delta_z
-        if np.iscomplexobj(dz):
-            raise NotImplementedError("DDGPE with a complex delta_z")
+        dz = self.delta_z  # complex for imaginary-time steps (nlse.py:505-508)
         g, g2, g12 = pf(self.g, "g"), pf(self.g2, "g2"), pf(self.g12, "g12")
         is1, is2 = pf(self.I_sat, "Isat"), pf(self.I_sat2, "Isat2")
         ga1, ga2 = pf(_host(self.gamma) / 2, "gamma"), pf(_host(self.gamma2) / 2, "gamma2")
@@ -173,7 +173,8 @@ class DDGPE(CNLSE):
 
         def put(set_, comp, dzs, a, gs, vs):
             o = set_ * 16 + comp * 7
-            P[:, o:o + 7] = np.stack([dzs * one, a, gs, g12, is1, is2, vs * one], axis=1)
+            P[:, o:o + 7] = np.stack([np.real(dzs) * one, a, gs, g12, is1, is2, vs * one], axis=1)
+            P[:, 32 + set_] = np.imag(dzs)
 
         if precision == "double":
             if not has_v:  # ddgpe.py:300-321 and 366-387
@@ -194,9 +195,12 @@ class DDGPE(CNLSE):
                 put(0, 1, dz, ga2, g2, 1.0)
         if self.omega is not None:
             w = pf(_host(self.omega) / 2, "omega")
-            P[:, 14] = np.cos(w * dz)
-            P[:, 15] = np.sin(w * dz)
-        P[:, 30] = dz
+            # the reference's cp.cos / cp.sin of the step, complex for a complex
+            # step (kernels_gpu.py:155-156)
+            cw, sw = np.cos(w * dz), np.sin(w * dz)
+            P[:, 14], P[:, 15] = np.real(cw), np.real(sw)
+            P[:, 34], P[:, 35] = np.imag(cw), np.imag(sw)
+        P[:, 30], P[:, 31] = np.real(dz), np.imag(dz)
         return P
 
     def _split_fused_callbacks(self, callback, callback_args, A):

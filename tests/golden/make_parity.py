@@ -17,8 +17,10 @@ Parts (each writes .npz files under tests/golden/):
   ddgpe128  the four DDGPE cases with complex128 fields and pump profiles
             -> ddgpe_c128_<branch>.npz
             (replayed by the golden tests like every other fixture).
-  imagtime  CNLSE with Rabi coupling and a complex delta_z, complex128
-            -> cnlse_c128_single_rabi_cdz.npz (+ spread/).
+  imagtime  CNLSE with Rabi coupling and DDGPE (pump, probe, potential,
+            Rabi coupling) with a complex delta_z, complex128
+            -> cnlse_c128_single_rabi_cdz.npz, ddgpe_c128_single_V_cdz.npz
+            (+ spread/).
   maps      NLSE 2-D with n2, alpha and Isat varying over the grid -> maps_*.npz
             (golden fixtures; run before spread and short, which cover them).
   fullsize  the benchmark configurations at their stated sizes (outputs
@@ -167,25 +169,29 @@ def part_ddgpe128() -> None:
 
 
 def part_imagtime() -> None:
-    """CNLSE with Rabi coupling and a complex delta_z (imaginary-time
+    """CNLSE with Rabi coupling and DDGPE with a complex delta_z (imaginary-time
     evolution, NLSE/nlse.py:505-508): the cnlse_c128_single_rabi inputs with
-    dz = (1 - 0.4j) 5e-5 -- the reference's rabi_coupling then takes the
-    complex cosine and sine of the step (kernels_gpu.py:155-156)
-    -> cnlse_c128_single_rabi_cdz.npz and its spread/ entry."""
+    dz = (1 - 0.4j) 5e-5 and the ddgpe_c128_single_V inputs with dz =
+    (1 - 0.3j) 0.1/32 -- the reference's rabi_coupling then takes the complex
+    cosine and sine of the step (kernels_gpu.py:155-156) and the DDGPE source
+    term the complex product F dz i (ddgpe.py:155-156)
+    -> cnlse_c128_single_rabi_cdz.npz, ddgpe_c128_single_V_cdz.npz and their
+    spread/ entries."""
     gc, _ = _cases()
-    use_fft("scipy")
-    name = "cnlse_c128_single_rabi_cdz"
-    arrays = dict(gc.load("cnlse_c128_single_rabi"))
-    arrays["dz"] = np.array((1 - 0.4j) * 5e-5)
-    np.savez_compressed(HERE / f"{name}.npz", **{**arrays, "out": np.zeros(0)})
-    arrays["out"] = gc.run(name, "reference")
-    save(HERE / f"{name}.npz", **arrays)
-    outs = {}
-    for kind in ("numpy", "torch"):
-        use_fft(kind)
-        outs[f"out_{kind}"] = gc.run(name, "reference")
-    use_fft("scipy")
-    save(HERE / "spread" / f"{name}.npz", **outs)
+    for name, src, dz in (("cnlse_c128_single_rabi_cdz", "cnlse_c128_single_rabi", (1 - 0.4j) * 5e-5),
+                          ("ddgpe_c128_single_V_cdz", "ddgpe_c128_single_V", (1 - 0.3j) * 0.1 / 32)):
+        use_fft("scipy")
+        arrays = dict(gc.load(src))
+        arrays["dz"] = np.array(dz)
+        np.savez_compressed(HERE / f"{name}.npz", **{**arrays, "out": np.zeros(0)})
+        arrays["out"] = gc.run(name, "reference")
+        save(HERE / f"{name}.npz", **arrays)
+        outs = {}
+        for kind in ("numpy", "torch"):
+            use_fft(kind)
+            outs[f"out_{kind}"] = gc.run(name, "reference")
+        use_fft("scipy")
+        save(HERE / "spread" / f"{name}.npz", **outs)
 
 
 def part_maps() -> None:

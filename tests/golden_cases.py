@@ -148,7 +148,7 @@ def run(name: str, kind: str, upcast: bool = False, steps: int | None = None):
         sim = C["DDGPE"](gamma=0.07 / h, power=1.0, window=64.0, g=1e-2 / h, omega=5.07 / h,
                          T=2.0, omega_exc=1484.44 / h, omega_cav=1482.76 / h,
                          detuning=0.17 / h, k_z=27.0, NX=32, NY=32)
-        sim.delta_z = 0.1 / 32
+        sim.delta_z = complex(f["dz"][()]) if "dz" in f else 0.1 / 32
         if f["V"].size:
             sim.V = f["V"].copy()
         final = {}

@@ -11,6 +11,7 @@ torch = pytest.importorskip("torch")
 import nlse_gb300 as ng  # noqa: E402
 from oracle import nlse_oracle as orc  # noqa: E402
 from tests import cases  # noqa: E402
+from tests import golden_cases as gc  # noqa: E402
 
 
 @pytest.mark.parametrize("N", [64, 256])
@@ -72,17 +73,39 @@ def test_rabi_coupling_with_complex_step(dtype, tol):
     assert cases.rel_l2(got, ref) <= tol
 
 
-def test_complex_step_rejected_where_unsupported():
-    """DDGPE with a complex step raises (not built)."""
+def _ddgpe():
     H = 0.654
-    d = ng.DDGPE(gamma=0.07 / H, power=1.0, window=64.0, g=1e-2 / H, omega=5.07 / H, T=2.0,
-                 omega_exc=1484.44 / H, omega_cav=1482.76 / H, detuning=0.17 / H, k_z=27.0,
-                 NX=32, NY=32)
-    d.delta_z = -1j * 0.1 / 32
-    E = np.zeros((2, 32, 32), dtype=np.complex128)
-    n = 70
-    Fr = np.zeros((32, 32), dtype=np.complex128)
-    Ft = np.zeros(n, dtype=np.complex128)
-    with pytest.raises(NotImplementedError):
-        d.out_field(E, 0.1, d.laser_excitation, verbose=False, callback=[lambda *a: None],
-                    callback_args=[[Fr, Ft, Fr, Ft], []])
+    return ng.DDGPE(gamma=0.07 / H, power=1.0, window=64.0, g=1e-2 / H, omega=5.07 / H, T=2.0,
+                    omega_exc=1484.44 / H, omega_cav=1482.76 / H, detuning=0.17 / H, k_z=27.0,
+                    NX=32, NY=32)
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_ddgpe_complex_step_matches_the_reference(fused):
+    """DDGPE (pump, probe, potential, Rabi coupling) with a complex step against
+    the reference's own complex128 result (ddgpe_c128_single_V_cdz): the
+    source term's complex product F dz i in the row pass (fused) or in the
+    host callback."""
+    f = gc.load("ddgpe_c128_single_V_cdz")
+    d = _ddgpe()
+    d.delta_z = complex(f["dz"][()])
+    d.V = f["V"].copy()
+    final = {}
+
+    def grab(simu, A, z, i):
+        final["A"] = A.clone()
+
+    cb = d.laser_excitation if fused else (lambda *a: ng.DDGPE.laser_excitation(*a))
+    d.out_field(f["E_in"].copy(), 2.0, cb, verbose=False, callback=[grab],
+                callback_args=[[f["Fr"], f["Ft"], f["Pr"], f["Pt"]], []])
+    assert cases.rel_l2(final["A"].cpu().numpy(), f["out"]) <= 1e-12
+
+
+def test_ddgpe_noise_with_complex_step_raises_like_the_reference():
+    """add_noise draws with scale = delta_z (ddgpe.py:114-119): a complex step
+    is rejected there, as NumPy's and CuPy's normal reject a complex scale."""
+    d = _ddgpe()
+    d.delta_z = (1 - 0.3j) * 0.1 / 32
+    A = torch.zeros((2, 32, 32), dtype=torch.complex64, device="cuda")
+    with pytest.raises(TypeError):
+        ng.DDGPE.add_noise(d, A, 0.0, 0, noise=1.0)
