@@ -464,8 +464,10 @@ def run_gb300(args):
                "h2d_bytes_per_step": int(h2d / nst), "d2h_bytes_per_step": int(out.numpy().nbytes / nst),
                "steps_per_call": nst, "calls": len(tes),
                "note": "out_field calls from pinned host memory to a new host tensor, median "
-                       "of 5 calls (the batch goes through out_field's copy/compute pipeline: "
-                       "4 field chunks, uploads and downloads overlapping the propagation); "
+                       "of 5 calls (loops of at most 100 steps go through out_field's "
+                       "copy/compute pipeline: the first and the last field alone, the others "
+                       "together, uploads and downloads overlapping the propagation; longer "
+                       "loops run unsplit); "
                        "h2d/d2h bytes per call divided by its steps"}
         # single 2048^2 field, the configuration's own 501-step loop (L2-resident)
         s1 = ng.NLSE(ALPHA, POWER, 4 * WAIST, N2, None, L, NX=N, NY=N, Isat=ISAT)

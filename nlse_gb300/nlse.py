@@ -461,8 +461,10 @@ class NLSE:
         in_dtype = E_in.dtype
         assert in_dtype in (np.complex64, np.complex128, torch.complex64, torch.complex128), (
             "Type mismatch, E_in should be complex64 or complex128")
-        if callback is None and self._pipeline_chunks(E_in) > 1:
-            return self._out_field_pipelined(E_in, z, precision, verbose, normalize)
+        if callback is None:
+            bounds = self._pipeline_bounds(E_in, count_steps(z, self.delta_z))
+            if bounds is not None:
+                return self._out_field_pipelined(E_in, z, precision, verbose, normalize, bounds)
         if self.propagator is None:
             self.propagator = self._build_propagator()
         self._send_arrays_to_gpu()
@@ -563,25 +565,34 @@ class NLSE:
     # host batches of at least this size go through the copy/compute pipeline
     PIPELINE_MIN_BYTES = 64 << 20
 
-    def _pipeline_chunks(self, E_in) -> int:
-        """Chunks of the host-to-host pipeline for this input (1: not pipelined).
+    # Longest loop that is pipelined: the pipeline hides the host link (268 MB
+    # each way for 8 fields of 2048^2 complex64: 1.3 ms up, 1.45 ms down) but
+    # runs its chunks at a smaller batch, which costs more per step than a
+    # whole-batch loop; for that batch the two break even near 120 steps
+    # (20 steps: 9.6 against 11.8 ms per call; 200 steps: 78.7 against 77.1).
+    PIPELINE_MAX_STEPS = 100
+
+    def _pipeline_bounds(self, E_in, nsteps: int):
+        """Field bounds of the host-to-host pipeline's chunks, or None.
 
         A page-locked host batch of 2-D fields (this class, no nonlocal
-        response) of at least PIPELINE_MIN_BYTES is split by fields: its
-        chunks' uploads, propagations and downloads overlap."""
-        if type(self) is not NLSE or self.nl_length > 0:
-            return 1
+        response) of at least PIPELINE_MIN_BYTES, propagated over at most
+        PIPELINE_MAX_STEPS steps, is split by fields: the first and the last
+        field alone, the others together, so that only one field's upload
+        and one field's download are not hidden behind a propagation."""
+        if type(self) is not NLSE or self.nl_length > 0 or nsteps > self.PIPELINE_MAX_STEPS:
+            return None
         if not (isinstance(E_in, torch.Tensor) and not E_in.is_cuda and E_in.is_pinned()
                 and E_in.is_contiguous()):
-            return 1
+            return None
         lead = self._lead_shape(tuple(E_in.shape))
         nf = int(np.prod(lead)) if lead else 1
         if nf < 2 or E_in.numel() * E_in.element_size() < self.PIPELINE_MIN_BYTES:
-            return 1
-        return 4 if nf >= 8 else 2
+            return None
+        return [0, 1, nf] if nf < 4 else [0, 1, nf - 1, nf]
 
     def _out_field_pipelined(self, E_in: torch.Tensor, z: float, precision: str, verbose: bool,
-                             normalize: bool) -> torch.Tensor:
+                             normalize: bool, bounds: list) -> torch.Tensor:
         """out_field of a page-locked host batch with the host link and the
         device overlapped: the batch is split into field chunks; chunk i is
         uploaded on one stream, normalised and propagated (its own plan and
@@ -598,8 +609,6 @@ class NLSE:
         lead = self._lead_shape(shape)
         nf = int(np.prod(lead))
         grid = shape[len(lead):]
-        nchunks = self._pipeline_chunks(E_in)
-        bounds = [nf * i // nchunks for i in range(nchunks + 1)]
         host_in = E_in.reshape(nf, *grid)
         A = torch.empty((nf, *grid), dtype=E_in.dtype, device=dev)
         stage = torch.empty_like(A) if normalize else A
@@ -607,6 +616,7 @@ class NLSE:
         dtype = engine.dtype_code(A)
         plans = [Plan.get(2, grid, b1 - b0, 1, dtype, dev, slot=i)
                  for i, (b0, b1) in enumerate(zip(bounds, bounds[1:]))]
+        big = max(range(len(plans)), key=lambda i: bounds[i + 1] - bounds[i])
         cur = torch.cuda.current_stream(dev)
         s_in, s_out = _pipeline_streams(dev)
         start = torch.cuda.Event(enable_timing=True)
@@ -640,11 +650,13 @@ class NLSE:
                     engine.normalize(stage[b0:b1], Ac, b1 - b0, sums, target[b0:b1],
                                      self._norm_coef())
                 if n > 0:
-                    if i == 0:
-                        autotune.maybe_tune(plans[0], Ac, op)
-                    else:
-                        # every chunk runs the first chunk's kernel variant
-                        v = plans[0].get_variant()
+                    # every chunk runs the kernel variant tuned for the largest
+                    # one (tuned once per process, on that chunk's buffer)
+                    if not getattr(plans[big], "_tuned", False):
+                        cur.wait_event(loaded[big])
+                        autotune.maybe_tune(plans[big], A[bounds[big]:bounds[big + 1]], op)
+                    if i != big:
+                        v = plans[big].get_variant()
                         plans[i].set_variant(v["rows"], v["cols"], v["rows_cap"], v["cols_cap"])
                     engine.propagate(plans[i], Ac, op, n, 0, graph=True, field0=b0)
                 done = torch.cuda.Event()

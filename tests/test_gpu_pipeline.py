@@ -33,17 +33,19 @@ def _sim(N, B, per_field, seed):
     return sim, E.astype(np.complex64)
 
 
-@pytest.mark.parametrize("N,B,per_field,chunks", [(1024, 8, True, 4), (2048, 3, False, 2),
-                                                   (1024, 9, False, 4)])
-def test_pipelined_host_batch_equals_device_call(N, B, per_field, chunks, monkeypatch):
+@pytest.mark.parametrize("N,B,per_field,bounds", [(1024, 8, True, [0, 1, 7, 8]),
+                                                   (2048, 3, False, [0, 1, 3]),
+                                                   (1024, 9, False, [0, 1, 8, 9])])
+def test_pipelined_host_batch_equals_device_call(N, B, per_field, bounds, monkeypatch):
     monkeypatch.setenv("NLSE_AUTOTUNE", "0")
     z = 11.5 * 5e-5
     sim, E = _sim(N, B, per_field, N + B)
     Eh = torch.from_numpy(E).pin_memory()
-    assert sim._pipeline_chunks(Eh) == chunks
+    assert sim._pipeline_bounds(Eh, ng.count_steps(z, sim.delta_z)) == bounds
+    # loops longer than PIPELINE_MAX_STEPS run unsplit (whole-batch kernels)
+    assert sim._pipeline_bounds(Eh, sim.PIPELINE_MAX_STEPS + 1) is None
     # every plan involved on one variant: the pipelined fields are the unsplit call's
     dev = torch.device("cuda", 0)
-    bounds = [B * i // chunks for i in range(chunks + 1)]
     plans = [engine.Plan.get(2, (N, N), b1 - b0, 1, _lib.NLSE_C64, dev, slot=i)
              for i, (b0, b1) in enumerate(zip(bounds, bounds[1:]))]
     plans.append(engine.Plan.get(2, (N, N), B, 1, _lib.NLSE_C64, dev))
@@ -60,5 +62,5 @@ def test_pipelined_host_batch_equals_device_call(N, B, per_field, chunks, monkey
     other = sim.out_field(Eh, z, verbose=False)
     assert cases.rel_l2(other.numpy(), ref.numpy()) <= 1e-5
     # a pageable NumPy batch takes the unsplit path and agrees as well
-    assert sim._pipeline_chunks(E) == 1
+    assert sim._pipeline_bounds(E, 12) is None
     np.testing.assert_array_equal(sim.out_field(E, z, verbose=False), ref.numpy())
