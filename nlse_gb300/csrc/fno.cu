@@ -696,42 +696,64 @@ __global__ void __launch_bounds__(256, 3) k_lift_rows(const LiftArgs a) {
     for (int i = p; i < kBasisAna / 8; i += 256) reinterpret_cast<uint4*>(sBa)[i] = g4[i];
   }
   __syncthreads();  // sWl
-  // row i: stage and TMEM columns (i & 1); its MMAs run while row i - 1 is read out
-  float x0 = 0.f, x1 = 0.f, x2 = 0.f;
-  {
-    const float* xi = a.xin + ((int64_t)blockIdx.x * N + p) * 3;
-    x0 = xi[0];
-    x1 = xi[1];
-    x2 = xi[2];
+  // thread: channel octet c8 of pixel x' of each quarter (x = 64 q + x'), the
+  // lift weights of its 8 channels for the three pixel inputs in registers
+  const int xq = p & (QW - 1), c8 = p / QW;
+  float w0[8], w1[8], w2[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    w0[j] = sWl[8 * c8 + j];
+    w1[j] = sWl[C + 8 * c8 + j];
+    w2[j] = sWl[2 * C + 8 * c8 + j];
   }
+  // row i: stage and TMEM columns (i & 1); its MMAs run while row i - 1 is read out
+  float xr[4][3];
+  auto load_x = [&](int64_t row) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float* xi = a.xin + (row * N + q * QW + xq) * 3;
+      xr[q][0] = xi[0];
+      xr[q][1] = xi[1];
+      xr[q][2] = xi[2];
+    }
+  };
+  load_x(blockIdx.x);
   bool ok = true;
   int it = 0;
   int64_t prev = -1;
   for (int64_t row = blockIdx.x; row < a.nrows; row += gridDim.x, ++it) {
     const int64_t b = row / N;
     const float s0 = a.xs[2 * b], s1 = a.xs[2 * b + 1];
-    float v[32];
+    float cst[8];  // bl + s0 wl[3] + s1 wl[4]: the field's part
 #pragma unroll
-    for (int o = 0; o < C; o += 4) {
-      float4 w[6];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) w[i] = *reinterpret_cast<const float4*>(sWl + i * C + o);
-      v[o] = w[5].x + x0 * w[0].x + x1 * w[1].x + x2 * w[2].x + s0 * w[3].x + s1 * w[4].x;
-      v[o + 1] = w[5].y + x0 * w[0].y + x1 * w[1].y + x2 * w[2].y + s0 * w[3].y + s1 * w[4].y;
-      v[o + 2] = w[5].z + x0 * w[0].z + x1 * w[1].z + x2 * w[2].z + s0 * w[3].z + s1 * w[4].z;
-      v[o + 3] = w[5].w + x0 * w[0].w + x1 * w[1].w + x2 * w[2].w + s0 * w[3].w + s1 * w[4].w;
+    for (int j = 0; j < 8; j += 4) {
+      const float4 bq = *reinterpret_cast<const float4*>(sWl + 5 * C + 8 * c8 + j);
+      const float4 w3 = *reinterpret_cast<const float4*>(sWl + 3 * C + 8 * c8 + j);
+      const float4 w4 = *reinterpret_cast<const float4*>(sWl + 4 * C + 8 * c8 + j);
+      cst[j] = fmaf(s1, w4.x, fmaf(s0, w3.x, bq.x));
+      cst[j + 1] = fmaf(s1, w4.y, fmaf(s0, w3.y, bq.y));
+      cst[j + 2] = fmaf(s1, w4.z, fmaf(s0, w3.z, bq.z));
+      cst[j + 3] = fmaf(s1, w4.w, fmaf(s0, w3.w, bq.w));
     }
-    const Bf16x32 hb = pack_bf16x32(v);  // h0 = bf16(lift)
-    const int64_t next = row + gridDim.x;
-    if (next < a.nrows) {
-      const float* xi = a.xin + (next * N + p) * 3;
-      x0 = xi[0];
-      x1 = xi[1];
-      x2 = xi[2];
-    }
-    store_packed(a.h0 + (row * N + p) * C, hb);
     unsigned char* stage = smraw + kLfStage + (it & 1) * kStageBytes;
-    stage_analysis(stage, p, hb);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t wd[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        const float v0 = fmaf(xr[q][2], w2[j], fmaf(xr[q][1], w1[j], fmaf(xr[q][0], w0[j], cst[j])));
+        const float v1 = fmaf(xr[q][2], w2[j + 1],
+                              fmaf(xr[q][1], w1[j + 1], fmaf(xr[q][0], w0[j + 1], cst[j + 1])));
+        const __nv_bfloat162 hb2 = __floats2bfloat162_rn(v0, v1);  // h0 = bf16(lift)
+        wd[j / 2] = *reinterpret_cast<const uint32_t*>(&hb2);
+      }
+      const uint4 hq = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+      *reinterpret_cast<uint4*>(a.h0 + (row * N + q * QW + xq) * C + 8 * c8) = hq;
+      *reinterpret_cast<uint4*>(stage + (xq >> 3) * kStageKStride + (q * 4 + c8) * 128 +
+                                (xq & 7) * 16) = hq;
+    }
+    const int64_t next = row + gridDim.x;
+    if (next < a.nrows) load_x(next);
     const uint32_t tbase = tc2_ready(st);
     if (p == 0) {
       issue_analysis_async(tbase + (it & 1) * KS, stage, sBa);
