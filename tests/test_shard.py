@@ -3,7 +3,7 @@ batch into whole-field blocks, "advance" their own block, and gather the batch;
 every rank must end with every field, in order, exactly once."""
 
 import os
-import socket
+import tempfile
 
 import torch
 import torch.multiprocessing as mp
@@ -21,18 +21,12 @@ def test_blocks_partition_the_batch():
             assert max(sizes) - min(sizes) <= 1
 
 
-def _free_port():
-    with socket.socket() as s:
-        s.bind(("127.0.0.1", 0))
-        return s.getsockname()[1]
-
-
-def _rank(rank, world, port, n, q):
+def _rank(rank, world, store_file, n, q):
     import torch.distributed as dist
 
-    os.environ["MASTER_ADDR"] = "127.0.0.1"
-    os.environ["MASTER_PORT"] = str(port)
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # a file rendezvous: no port to race for with other processes
+    dist.init_process_group("gloo", init_method=f"file://{store_file}", rank=rank,
+                            world_size=world)
     try:
         blk = field_block(n, rank, world)
         fields = torch.arange(n * 6, dtype=torch.float64).reshape(n, 3, 2)
@@ -47,8 +41,8 @@ def test_two_gloo_ranks_gather_every_field_once():
     n, world = 7, 2
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, world, port, n, q)) for r in range(world)]
+    store_file = os.path.join(tempfile.mkdtemp(prefix="nlse_gloo_"), "store")
+    procs = [ctx.Process(target=_rank, args=(r, world, store_file, n, q)) for r in range(world)]
     for p in procs:
         p.start()
     results = [q.get(timeout=120) for _ in range(world)]
