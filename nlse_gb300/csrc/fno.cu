@@ -284,48 +284,102 @@ __device__ __forceinline__ int chunk_of(int r, int k8, int K) {
 }
 
 // ---- per-mode channel mixing on tensor cores ---------------------------------
-// Y[m][b][:] = X[m][b][:] . Wbig[m] in the real 64 x 64 form (Re | Im); one CTA
-// per (mode, 128-row tile); rows at or beyond nb are zero.
+// Y[m][b][:] = X[m][b][:] . Wbig[m] in the real 64 x 64 form (Re | Im) for
+// every item (mode m, 128-row tile mt), item = m * nmt + mt.  Persistent: a
+// CTA walks items blockIdx.x, + gridDim.x, ...; both operands are stored in
+// the tensor-core layout, so each arrives by two bulk copies, two items ahead
+// of its product (stages alternate).  Rows at or beyond nb are multiplied
+// from whatever the tile holds there and not stored (a product row depends
+// only on its own A row).
+constexpr size_t kMixStage = (size_t)(XTILE + WBIG) * 2;  // bytes of one item's operands
+constexpr size_t kMixSmem = 2 * kMixStage + 4 * sizeof(uint64_t) + sizeof(uint32_t);
+static_assert(kMixStage % 128 == 0 && (XTILE * 2) % 128 == 0, "mixing operand alignment");
+
 __global__ void __launch_bounds__(128) k_mix(const __nv_bfloat16* __restrict__ Xc,
                                               const __nv_bfloat16* __restrict__ Wbig, int nb, int nmt,
                                               float2* __restrict__ Y, int* status) {
-  __shared__ __align__(128) __nv_bfloat16 sA[XTILE];
-  __shared__ __align__(128) __nv_bfloat16 sB[WBIG];
-  __shared__ TcState st;
-  const int m = blockIdx.x / nmt, mt = blockIdx.x % nmt;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smraw + 2 * kMixStage);  // operands landed, per stage
+  uint64_t* done = full + 2;                                             // product complete, per stage
+  uint32_t* taddr = reinterpret_cast<uint32_t*>(done + 2);
   const int tid = threadIdx.x, warp = tid >> 5;
-  tc_begin(&st, 64);
-  const uint4* gA = reinterpret_cast<const uint4*>(Xc + ((int64_t)m * nmt + mt) * XTILE);
-  uint4* sA4 = reinterpret_cast<uint4*>(sA);
-  for (int i = tid; i < XTILE / 8; i += 128) {
-    const int r = (i >> 6) * 8 + (i & 7);  // chunk i = (r/8)*64 + k8*8 + r%8
-    sA4[i] = (mt * TILE_M + r < nb) ? gA[i] : make_uint4(0, 0, 0, 0);
-  }
-  const uint4* gB = reinterpret_cast<const uint4*>(Wbig + (int64_t)m * WBIG);
-  uint4* sB4 = reinterpret_cast<uint4*>(sB);
-  for (int i = tid; i < WBIG / 8; i += 128) sB4[i] = gB[i];
-  const uint32_t tbase = tc_operands_ready(&st);
+  const unsigned items = (unsigned)NM * (unsigned)nmt;
+  if (blockIdx.x >= items) return;
+  if (warp == 0) tmem_alloc(taddr, 64);
   if (tid == 0) {
-    const uint32_t idesc = umma_idesc_bf16(TILE_M, XK);
-    const uint32_t a0 = smem_addr(sA), b0 = smem_addr(sB);
-#pragma unroll
-    for (int kk = 0; kk < XK / 16; ++kk)
-      umma_bf16(tbase, umma_desc(a0 + kk * 256, kUmmaLbo, umma_sbo(XK)),
-                umma_desc(b0 + kk * 256, kUmmaLbo, umma_sbo(XK)), idesc, kk);
-    umma_commit(&st.bar);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&done[i], 1);
+    }
+    mbar_init_fence();
   }
-  if (tc_wait(&st, status)) {
+  auto issue = [&](int st, unsigned item) {
+    const unsigned m = item / (unsigned)nmt, mt = item % (unsigned)nmt;
+    unsigned char* dst = smraw + st * kMixStage;
+    mbar_arrive_expect_tx(&full[st], (unsigned)kMixStage);
+    bulk_load(dst, Xc + ((int64_t)m * nmt + mt) * XTILE, XTILE * 2, &full[st]);
+    bulk_load(dst + XTILE * 2, Wbig + (int64_t)m * WBIG, WBIG * 2, &full[st]);
+  };
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  const uint32_t tbase = *taddr;
+  if (tid == 0) {
+    issue(0, blockIdx.x);
+    if (blockIdx.x + gridDim.x < items) issue(1, blockIdx.x + gridDim.x);
+  }
+  const uint32_t idesc = umma_idesc_bf16(TILE_M, XK);
+  int it = 0;
+  for (unsigned item = blockIdx.x; item < items; item += gridDim.x, ++it) {
+    const int st = it & 1;
+    const unsigned par = (unsigned)((it >> 1) & 1);
+    const unsigned ahead = item + gridDim.x;  // in flight into the other stage
+    // this item's operands have landed; every thread's read-out of the
+    // previous product is complete (fenced before the barrier)
+    if (!__syncthreads_and(mbar_wait_bounded(&full[st], par))) {
+      if (tid == 0) {
+        atomicExch(status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&full[st], par);
+        if (ahead < items) mbar_wait_bounded(&full[st ^ 1], (unsigned)(((it + 1) >> 1) & 1));
+      }
+      break;
+    }
+    tc_fence_after_sync();
+    if (tid == 0) {
+      const uint32_t a0 = smem_addr(smraw + st * kMixStage);
+      const uint32_t b0 = a0 + XTILE * 2;
+#pragma unroll
+      for (int kk = 0; kk < XK / 16; ++kk)
+        umma_bf16(tbase, umma_desc(a0 + kk * 256, kUmmaLbo, umma_sbo(XK)),
+                  umma_desc(b0 + kk * 256, kUmmaLbo, umma_sbo(XK)), idesc, kk);
+      umma_commit(&done[st]);
+    }
+    if (!__syncthreads_and(mbar_wait_bounded(&done[st], par))) {
+      if (tid == 0) {
+        atomicExch(status, DEV_WAIT_TIMEOUT);
+        mbar_wait_bounded(&done[st], par);
+        if (ahead < items) mbar_wait_bounded(&full[st ^ 1], (unsigned)(((it + 1) >> 1) & 1));
+      }
+      break;
+    }
+    tc_fence_after_sync();
+    // the product has read this stage: the item two ahead goes into it
+    if (tid == 0 && ahead + gridDim.x < items) issue(st, ahead + gridDim.x);
+    const unsigned m = item / (unsigned)nmt, mt = item % (unsigned)nmt;
     float re[32], im[32];
     tmem_ld32(tmem_lane_addr(tbase, warp, 0), re);
     tmem_ld32(tmem_lane_addr(tbase, warp, 32), im);
-    const int b = mt * TILE_M + warp * 32 + (tid & 31);
+    const int b = (int)mt * TILE_M + warp * 32 + (tid & 31);
     if (b < nb) {
       float4* dst = reinterpret_cast<float4*>(Y + ((int64_t)m * nb + b) * C);
 #pragma unroll
       for (int o = 0; o < C; o += 2) dst[o / 2] = make_float4(re[o], im[o], re[o + 1], im[o + 1]);
     }
+    tc_fence_before_sync();  // the next product overwrites the accumulator
   }
-  tc_end(&st, tbase, 64);
+  tc_fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, 64);
 }
 
 // ---- row analysis and synthesis as tensor-core contractions -----------------
@@ -1175,6 +1229,7 @@ bool g_attr_done[64] = {};
 const __nv_bfloat16* g_basis[64] = {};
 int g_layer_ctas[64] = {};  // resident k_layer_rows CTAs of the device
 int g_lift_ctas[64] = {};   // resident k_lift_rows CTAs of the device
+int g_mix_ctas[64] = {};    // resident k_mix CTAs of the device
 
 uint16_t host_bf16_bits(double v) {
   // double -> float (nearest) -> bfloat16 (nearest, ties to even)
@@ -1232,6 +1287,8 @@ int prepare(const float2** tw) {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_lift_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)kLiftBwdSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMixSmem);
     if (e != cudaSuccess) return shared_cuda_fail(e, "cudaFuncSetAttribute (FNO kernels)");
     // persistent grids: every CTA the multiprocessors can hold (shared memory,
     // registers and threads counted here from the kernels' attributes)
@@ -1246,20 +1303,23 @@ int prepare(const float2** tw) {
     if (e == cudaSuccess)
       e = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
     if (e != cudaSuccess) return shared_cuda_fail(e, "device attributes");
-    auto resident = [&](const void* fn, size_t smem, int* out) {
+    auto resident = [&](const void* fn, size_t smem, int threads, int* out) {
       cudaFuncAttributes fa;
       const cudaError_t fe = cudaFuncGetAttributes(&fa, fn);
       if (fe != cudaSuccess) return fe;
-      const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * 8;  // 8 warps, 256-register units
+      // registers are granted per warp in units of 256
+      const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * (threads / 32);
       int n = (int)(smem_sm / (smem + fa.sharedSizeBytes + smem_res));
       if (regs_cta > 0 && regs_sm / regs_cta < n) n = regs_sm / regs_cta;
-      if (thr_sm / 256 < n) n = thr_sm / 256;
+      if (thr_sm / threads < n) n = thr_sm / threads;
       *out = nsm * (n > 0 ? n : 1);
       return cudaSuccess;
     };
-    e = resident(reinterpret_cast<const void*>(k_layer_rows), kLayerSmem, &g_layer_ctas[dev]);
+    e = resident(reinterpret_cast<const void*>(k_layer_rows), kLayerSmem, 256, &g_layer_ctas[dev]);
     if (e == cudaSuccess)
-      e = resident(reinterpret_cast<const void*>(k_lift_rows), kLiftSmem, &g_lift_ctas[dev]);
+      e = resident(reinterpret_cast<const void*>(k_lift_rows), kLiftSmem, 256, &g_lift_ctas[dev]);
+    if (e == cudaSuccess)
+      e = resident(reinterpret_cast<const void*>(k_mix), kMixSmem, 128, &g_mix_ctas[dev]);
     if (e != cudaSuccess) return shared_cuda_fail(e, "persistent grid sizes");
     const int brc = make_basis(dev);
     if (brc != NLSE_OK) return brc;
@@ -1331,8 +1391,15 @@ int nlse_fno_mix(int64_t nb, const void* Xc, const void* wbig, void* Y, int32_t*
   if (bad_batch(nb) || !Xc || !wbig || !Y || !status)
     return nlse::shared_fail(NLSE_ERR_ARG, "nlse_fno_mix: bad argument");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const float2* tw;
+  int rc = prepare(&tw);
+  if (rc != NLSE_OK) return rc;
   const int nmt = nmt_of(nb);
-  k_mix<<<(unsigned)(NM * nmt), 128, 0, s>>>(reinterpret_cast<const __nv_bfloat16*>(Xc),
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int64_t items = (int64_t)NM * nmt;
+  const int64_t grid = items < g_mix_ctas[dev] ? items : g_mix_ctas[dev];
+  k_mix<<<(unsigned)grid, 128, kMixSmem, s>>>(reinterpret_cast<const __nv_bfloat16*>(Xc),
                                               reinterpret_cast<const __nv_bfloat16*>(wbig), (int)nb,
                                               nmt, reinterpret_cast<float2*>(Y), status);
   return launched("nlse_fno_mix");
