@@ -10,15 +10,20 @@
 //             the row spectra as bf16(U / N^2), FP32 sums)
 //   S_l(k)  = bf16(H_l(k)) . bf16(W_l(k))        per-mode 32 x 32 complex mixing
 //   H_l(k)  = sum_x h_l(x) exp(-2 pi i k.x / N)  truncated transform
+//             (its row stage as a BF16 contraction over quarter rows:
+//             bf16(cos), bf16(sin) of 2 pi kx x'/N, exact (-i)^(kx q), FP32 sums)
 //   h_{l+1} = bf16(GELU(z_l)) (l < 3),  h_4 = bf16(z_3)   GELU in its tanh form
 //   out     = h_4 . Wp + bp                      two channels: Re, Im of E(L)
-// The truncated transforms run on the project's Stockham FFT (fft_core.cuh):
-// 256-point row transforms of channel pairs packed as one complex line, and
-// 256-point column transforms of the kept kx.  Both contractions (mode mixing
-// and 1 x 1 convolution, forward and backward) are BF16 x BF16 -> FP32 tcgen05
-// MMAs with the accumulator in tensor memory (umma.cuh); weight gradients are
-// FP32 reductions on the CUDA cores.  Rounding steps pass gradients through
-// unchanged.  No reference counterpart: the surrogate is new to this project.
+// Forward: the row stages of both truncated transforms are tcgen05 BF16 x
+// BF16 -> FP32 contractions (the synthesis accumulated onto the 1 x 1
+// convolution), the column stages 256-point transforms of the kept kx on the
+// project's Stockham FFT (fft_core.cuh), the mode mixing a tcgen05 product per
+// mode.  Backward: the same mixing and convolution products; the row
+// transforms of the gradients on the FFT (256-point lines of channel pairs
+// packed as one complex line).  Accumulators live in tensor memory
+// (umma.cuh); weight gradients are FP32 reductions on the CUDA cores.
+// Rounding steps pass gradients through unchanged.  No reference
+// counterpart: the surrogate is new to this project.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
