@@ -57,7 +57,6 @@ constexpr int PS = 17;              // pair stride of the [pixel][channel pair] 
 constexpr size_t kPairBuf =
     (16 * SL > N * PS ? 16 * SL : N * PS) * sizeof(float2);  // shared by xl and the pairs
 
-__device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 // GELU in its tanh form, 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3),
 // with the hardware tanh (relative error ~2^-11, below the BF16 rounding of
 // the stored activations)
@@ -78,15 +77,6 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // kept row iy (0..63) of ky
 __device__ __forceinline__ int iy_of(int ky) { return ky < KY / 2 ? ky : ky - (N - KY); }
 
-__device__ __forceinline__ void store_bf16x32(__nv_bfloat16* dst, const float (&v)[32]) {
-  __align__(16) __nv_bfloat16 b[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) b[i] = __float2bfloat16_rn(v[i]);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  const uint4* s = reinterpret_cast<const uint4*>(b);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) d[i] = s[i];
-}
 
 __device__ __forceinline__ void load_bf16x32(const __nv_bfloat16* src, float (&v)[32]) {
   __align__(16) __nv_bfloat16 b[32];
