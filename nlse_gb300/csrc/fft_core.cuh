@@ -111,11 +111,6 @@ template <typename T>
 __device__ __forceinline__ cpx<T> cscale(cpx<T> a, T s) {
   return mk<T>(a.x * s, a.y * s);
 }
-// a * (-i) for the forward transform, a * (+i) for the inverse.
-template <typename T, bool INV>
-__device__ __forceinline__ cpx<T> mul_mi(cpx<T> a) {
-  return INV ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);
-}
 // a * w where w = (wr, -wi) forward (exp(-i*theta)), (wr, +wi) inverse.
 template <typename T, bool INV>
 __device__ __forceinline__ cpx<T> mul_w(cpx<T> a, T wr, T wi) {
