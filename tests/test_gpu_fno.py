@@ -44,6 +44,42 @@ def test_tensor_core_gemm_selftest(n, k):
     np.testing.assert_allclose(C.cpu().numpy(), ref, rtol=1e-5, atol=1e-4)
 
 
+def _canonical(t):
+    """(..., R, K) -> the tensor-core operand layout (8 x 8 core matrices, K-adjacent
+    ones packed): element (r, k) at (r/8)*8K + (k/8)*64 + (r%8)*8 + k%8."""
+    *lead, R, K = t.shape
+    t = t.reshape(*lead, R // 8, 8, K // 8, 8)
+    return t.transpose(-3, -2).reshape(*lead, R * K)
+
+
+def test_mode_mixing_over_partial_tiles_matches_numpy():
+    """nlse_fno_mix on 130 fields (two 128-row tiles, the second holding 2):
+    every mode's product against NumPy; rows past the batch are NaN in the
+    operand and must not reach the stored rows."""
+    from nlse_gb300 import _lib
+
+    lib = _lib.load()
+    nb, NM, XK = 130, fo.NM, 2 * fo.C
+    nmt = (nb + 127) // 128
+    rng = np.random.default_rng(21)
+    A = torch.full((NM, nmt * 128, XK), float("nan"), dtype=torch.bfloat16)
+    A[:, :nb] = _bf16(rng.normal(size=(NM, nb, XK)))
+    B = _bf16(rng.normal(size=(NM, XK, XK)))
+    X = _canonical(A.reshape(NM, nmt, 128, XK)).contiguous().cuda()
+    Wb = _canonical(B).contiguous().cuda()
+    Y = torch.zeros((NM, nb, fo.C), dtype=torch.complex64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.check(lib.nlse_fno_mix(nb, X.data_ptr(), Wb.data_ptr(), Y.data_ptr(), st.data_ptr(),
+                                ct.c_void_p(torch.cuda.current_stream().cuda_stream)), "mix")
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    D = np.einsum("mbk,mnk->mbn", A[:, :nb].double().numpy(), B.double().numpy())
+    ref = D[..., :fo.C] + 1j * D[..., fo.C:]
+    got = Y.cpu().numpy()
+    assert np.isfinite(got).all()
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-4)
+
+
 def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
