@@ -92,8 +92,11 @@ def _net(flat):
     return net
 
 
-def test_forward_matches_oracle():
-    flat, xin, xs, _ = _problem(seed=5, B=3)
+@pytest.mark.parametrize("B", [1, 3])
+def test_forward_matches_oracle(B):
+    # B = 1: fewer image rows (256) than resident row-kernel CTAs; B = 3: each
+    # persistent CTA walks several rows
+    flat, xin, xs, _ = _problem(seed=5, B=B)
     flat = flat.astype(np.float32).astype(np.float64)
     xin, xs = xin.astype(np.float32), xs.astype(np.float32)
     net = _net(flat)
