@@ -490,12 +490,33 @@ int conv_nl(nlse_plan_s* p, void* A, const nlse_operator* op, int set, int64_t s
   const int64_t py = d.ndim == 2 ? p->nl_py : 1, px = p->nl_px;
   cudaError_t e = launch_pack_asq(d.dtype, d.comps, A, p->X, d.nfields, ny, nx, py, px, s);
   if (e != cudaSuccess) return cuda_fail(e, "nonlocal pack");
-  int rc = fft_sub(p->nlsub, p->X, 0, s);
-  if (rc != NLSE_OK) return rc;
-  e = launch_mul_spectrum(d.dtype, p->X, op->nl_khat, py * px, d.nfields * py * px, s);
-  if (e != cudaSuccess) return cuda_fail(e, "nonlocal spectrum");
-  rc = fft_sub(p->nlsub, p->X, 1, s);
-  if (rc != NLSE_OK) return rc;
+  if (d.ndim == 2) {
+    // forward rows; one column pass: forward transform, times the kernel
+    // spectrum (as a propagator), inverse transform; inverse rows with the
+    // 2-D transform's 1/N (the products and their rounding are those of the
+    // separate passes and spectrum multiply)
+    const nlse_plan_s* q = p->nlsub;
+    StepArgs ra = row_args(q, p->X, nullptr);
+    ra.flags = F_NO_POST;
+    const int rl = q->lg[1];
+    e = rows(q, ROW_FWD, rl, ra, s);
+    if (e == cudaSuccess) {
+      ColArgs ca = col_args(q, p->X, nullptr, 0);
+      ca.prop = op->nl_khat;
+      ca.prop_cstride = 0;
+      ca.flags = d.dtype == NLSE_C128 ? F_PROP_C128 : 0u;
+      e = cols(q, COL_FWD_PROP_INV, q->lg[0], ca, s);
+    }
+    if (e == cudaSuccess) e = rows(q, ROW_INV, rl, ra, s);
+    if (e != cudaSuccess) return cuda_fail(e, "nonlocal convolution");
+  } else {
+    int rc = fft_sub(p->nlsub, p->X, 0, s);
+    if (rc != NLSE_OK) return rc;
+    e = launch_mul_spectrum(d.dtype, p->X, op->nl_khat, py * px, d.nfields * py * px, s);
+    if (e != cudaSuccess) return cuda_fail(e, "nonlocal spectrum");
+    rc = fft_sub(p->nlsub, p->X, 1, s);
+    if (rc != NLSE_OK) return rc;
+  }
   StepArgs a = row_args(p, A, op);
   a.step = (int)step;
   if (set == 1) a.flags &= ~(F_RABI | F_PUMP | F_PROBE);
