@@ -39,6 +39,7 @@ SOURCES = [
     "rows_deep_mid.cu",
     "rows_deep_last.cu",
     "cols_deep.cu",
+    "nonlocal_rows.cu",
     "multi_pair.cu",
     "multi_rows_mid.cu",
     "multi_rows_last.cu",

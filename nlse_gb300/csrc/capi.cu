@@ -488,6 +488,29 @@ int conv_nl(nlse_plan_s* p, void* A, const nlse_operator* op, int set, int64_t s
   const nlse_desc& d = p->d;
   const int64_t ny = d.ndim == 2 ? d.shape[0] : 1, nx = d.shape[d.ndim - 1];
   const int64_t py = d.ndim == 2 ? p->nl_py : 1, px = p->nl_px;
+  const nlse_plan_s* q = p->nlsub;
+  if (d.ndim == 2 && nonlocal_rows_fused(d.dtype, q->lg[1], ny, py)) {
+    // |A|^2 packed inside the forward row pass; the spectrum multiply inside
+    // the column pass; the nonlinear step inside the inverse row pass of the
+    // field's rows
+    cudaError_t e = launch_pack_rows_fwd(q->lg[1], d.comps, A, p->X, d.nfields, ny, nx, py, q->tw, s);
+    if (e == cudaSuccess) {
+      ColArgs ca = col_args(q, p->X, nullptr, 0);
+      ca.prop = op->nl_khat;
+      ca.prop_cstride = 0;
+      ca.flags = 0u;
+      e = cols(q, COL_FWD_PROP_INV, q->lg[0], ca, s);
+    }
+    if (e == cudaSuccess) {
+      StepArgs a = row_args(p, A, op);
+      a.step = (int)step;
+      if (set == 1) a.flags &= ~(F_RABI | F_PUMP | F_PROBE);
+      e = launch_rows_inv_nl_pad(q->lg[1], a, p->X, ny, nx, py, set,
+                                 (float)(1.0 / ((double)py * (double)px)), s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "nonlocal convolution and nonlinear step");
+    return NLSE_OK;
+  }
   cudaError_t e = launch_pack_asq(d.dtype, d.comps, A, p->X, d.nfields, ny, nx, py, px, s);
   if (e != cudaSuccess) return cuda_fail(e, "nonlocal pack");
   if (d.ndim == 2) {
@@ -495,7 +518,6 @@ int conv_nl(nlse_plan_s* p, void* A, const nlse_operator* op, int set, int64_t s
     // spectrum (as a propagator), inverse transform; inverse rows with the
     // 2-D transform's 1/N (the products and their rounding are those of the
     // separate passes and spectrum multiply)
-    const nlse_plan_s* q = p->nlsub;
     StepArgs ra = row_args(q, p->X, nullptr);
     ra.flags = F_NO_POST;
     const int rl = q->lg[1];

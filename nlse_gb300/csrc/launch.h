@@ -81,6 +81,14 @@ cudaError_t launch_delta_n_max(int dtype, const void* A, int64_t nseg, int64_t p
 // kernel spectrum, nonlinear step reading the convolved intensities.
 cudaError_t launch_pack_asq(int dtype, int nc, const void* A, void* X, int64_t nfields, int64_t ny,
                             int64_t nx, int64_t py, int64_t px, cudaStream_t s);
+// Fused row passes of the nonlocal convolution (nonlocal_rows.cu): whether
+// they apply, |A|^2 packing + forward rows, inverse rows + the nonlinear step.
+bool nonlocal_rows_fused(int dtype, int log2px, int64_t ny, int64_t py);
+cudaError_t launch_pack_rows_fwd(int log2px, int nc, const void* A, void* X, int64_t nfields,
+                                 int64_t ny, int64_t nx, int64_t py, const void* tw,
+                                 cudaStream_t s);
+cudaError_t launch_rows_inv_nl_pad(int log2px, const StepArgs& a, const void* X, int64_t ny,
+                                   int64_t nx, int64_t py, int set, float inv_n, cudaStream_t s);
 cudaError_t launch_mul_spectrum(int dtype, void* X, const void* K, int64_t per, int64_t total,
                                 cudaStream_t s);
 cudaError_t launch_nl_pointwise_pad(int dtype, const StepArgs& a, const void* X, int64_t ny,

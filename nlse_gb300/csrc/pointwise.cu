@@ -5,6 +5,7 @@
 #include <type_traits>
 
 #include "launch.h"
+#include "nl_pad.cuh"
 
 namespace nlse {
 
@@ -186,61 +187,17 @@ __global__ void k_mul_spectrum(cpx<T>* __restrict__ X, const cpx<T>* __restrict_
     X[i] = cmul<T>(X[i], __ldg(K + i % per));
 }
 
-// Nonlinear step (parameter set 0) with |A|^2 taken from the convolved,
-// padded scratch X: component 0 from the real part, component 1 from the
-// imaginary part.
+// Nonlinear step (parameter set `set`) with |A|^2 taken from the convolved,
+// padded scratch X (nl_pad.cuh).
 template <typename T, int NC>
 __global__ void k_nl_point_pad(const StepArgs a, const cpx<T>* __restrict__ X, int64_t ny, int64_t nx,
                                int64_t py, int64_t px, int set) {
   const int64_t nf = a.nq / a.lines_per_comp;
   const int64_t total = nf * a.pix;
-  cpx<T>* A = reinterpret_cast<cpx<T>*>(a.A);
-  const bool has_v = a.flags & F_HAS_V;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = i / a.pix, pxl = i % a.pix, y = pxl / nx, x = pxl % nx;
-    const cpx<T> c = X[(f * py + y) * px + x];
-    const T* P = param_block<T>(a) + f * kParamStride + set * 16;
-    const int64_t i0 = (f * NC) * a.pix + pxl;
-    NLP<T> p0 = load_nlp<T>(P);
-    p0.dzi = param_block<T>(a)[f * kParamStride + 32 + set];
-    const int64_t vi = f * a.v_fstride + pxl;
-    const cpx<T> v0 = has_v ? load_vp<T>(a.V, a.flags, vi, p0.vs) : mk<T>(T(0), T(0));
-    if constexpr (NC == 1) {
-      if (a.flags & F_MAPS) apply_maps<T>(p0, a, f, pxl);
-      A[i0] = nl_point<T, false>(A[i0], c.x, T(0), p0, has_v, v0);
-    } else {
-      const int64_t i1 = i0 + a.pix;
-      NLP<T> p1 = load_nlp<T>(P + 7);
-      p1.dzi = p0.dzi;
-      const cpx<T> v1 = has_v ? load_vp<T>(a.V, a.flags, vi, p1.vs) : mk<T>(T(0), T(0));
-      cpx<T> y0 = nl_point<T>(A[i0], c.x, c.y, p0, has_v, v0);
-      cpx<T> y1 = nl_point<T>(A[i1], c.y, c.x, p1, has_v, v1);
-      if (a.flags & F_RABI) {
-        const T rc = P[14], rs = P[15], ric = P[34], ris = P[35];
-        const cpx<T> z0 = rabi_rot<T>(y0, y1, rc, rs, ric, ris);
-        const cpx<T> z1 = rabi_rot<T>(y1, y0, rc, rs, ric, ris);
-        y0 = z0;
-        y1 = z1;
-      }
-      if (a.flags & (F_PUMP | F_PROBE)) {
-        const T dz = P[30];
-        if (a.flags & F_PUMP) {
-          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.pump_r)[pxl],
-                             reinterpret_cast<const cpx<T>*>(a.pump_t)[a.step]);
-          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
-          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
-        }
-        if (a.flags & F_PROBE) {
-          cpx<T> u = cmul<T>(reinterpret_cast<const cpx<T>*>(a.probe_r)[pxl],
-                             reinterpret_cast<const cpx<T>*>(a.probe_t)[a.step]);
-          u = mk<T>(mul_rn(u.x, dz), mul_rn(u.y, dz));
-          y1 = mk<T>(y1.x + u.y, y1.y - u.x);
-        }
-      }
-      A[i0] = y0;
-      A[i1] = y1;
-    }
+    nl_pad_point<T, NC>(a, f, pxl, X[(f * py + y) * px + x], set);
   }
 }
 
