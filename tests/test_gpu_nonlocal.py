@@ -120,3 +120,30 @@ def test_nonlocality_conserves_power():
     g.delta_z = 1e-5
     E = g.out_field(E0, L, verbose=False)
     assert np.allclose((np.abs(E) ** 2).sum() * g.delta_X * g.delta_Y, g.N, rtol=1e-3)
+
+
+@pytest.mark.parametrize("cls_name,N", [("CNLSE", 256), ("CNLSE", 512), ("NLSE", 512),
+                                        ("CNLSE", 2048)])
+def test_fused_nonlocal_passes_match_the_complex128_run(cls_name, N):
+    """complex64 fields on padded grids of 512 to 4096 points per axis take the
+    fused nonlocal passes (packing + forward rows, columns x kernel spectrum,
+    inverse rows + nonlinear step); complex128 fields take the separate passes.
+    A few steps from the same input agree to complex64 rounding."""
+    waist = 1.5e-3
+    dx = 4 * waist / N
+    k = _gauss_kernel(100e-6 / dx, 10)  # 21 x 21: padded grid 2N
+    outs = {}
+    for dt in (np.complex64, np.complex128):
+        if cls_name == "CNLSE":
+            s = ng.CNLSE(20, 0.5, 4 * waist, -1.6e-9, -0.8e-9, None, 20e-3, NX=N, NY=N, Isat=1e5,
+                         nl_length=100e-6)
+            s.power2, s.n22 = 0.05, -1.6e-9
+            E = np.array([cases.gaussian(s.XX, s.YY, waist), cases.gaussian(s.XX, s.YY, 0.5 * waist)])
+        else:
+            s = ng.NLSE(20, 1.05, 4 * waist, -1.6e-9, None, 20e-3, NX=N, NY=N, Isat=1e5,
+                        nl_length=100e-6)
+            E = cases.gaussian(s.XX, s.YY, waist)
+        s.nl_profile = k
+        s.delta_z = 5e-5
+        outs[dt] = s.out_field(E.astype(dt), 4.5 * 5e-5, verbose=False)
+    assert cases.rel_l2(outs[np.complex64], outs[np.complex128]) <= 1e-5
