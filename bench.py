@@ -123,6 +123,9 @@ def parse():
     ap.add_argument("--mixed-only", action="store_true",
                     help="only time the 164-field mixed batch (--steps steps per call; for "
                          "profiling)")
+    ap.add_argument("--cnlse-only", type=int, default=0, metavar="STEPS",
+                    help="only run the CNLSE 1024^2 nonlocal configuration: three out_field "
+                         "calls of STEPS steps, the last one timed (for profiling)")
     ap.add_argument("--network-only", type=int, default=0, metavar="FIELDS",
                     help="only time the surrogate network's inference on FIELDS random "
                          "256^2 inputs (--steps passes after one warm-up; for profiling)")
@@ -515,16 +518,7 @@ def run_gb300(args):
                                "device memory, L2 flushed between loops"}
         # the coupled 1024^2 configuration: CNLSE, both components, Gaussian nonlocal
         # kernel (sigma 100 um on a 67^2 support), L = 20 mm at dz = 5e-5 (400 steps)
-        NC, LC = 1024, 20e-3
-        s3 = ng.CNLSE(ALPHA, 0.5, 4 * WAIST, N2, -0.8e-9, None, LC, NX=NC, NY=NC, Isat=ISAT,
-                      nl_length=100e-6)
-        s3.delta_z, s3.power2, s3.n22 = 5e-5, 0.05, N2
-        dxc = 4 * WAIST / NC
-        rr = np.arange(-33, 34) * dxc
-        kern = np.exp(-(rr[:, None] ** 2 + rr[None, :] ** 2) / (2 * (100e-6) ** 2))
-        s3.nl_profile = kern / kern.sum()
-        E3 = np.array([np.exp(-(s3.XX**2 + s3.YY**2) / w**2) for w in (1.5e-3, 0.5e-3)])
-        E3 = torch.from_numpy(E3.astype(np.complex64)).to(dev)
+        s3, E3, LC = cnlse_setup(dev)
         tc = loop_time(s3, E3, LC)
         nst3 = ng.count_steps(LC, 5e-5)
         cnlse = {"steps": nst3, "steps_per_s": nst3 / tc,
@@ -637,6 +631,48 @@ def mixed_only(args):
     print(json.dumps({"mixed_batch_164": mixed_batch_leg(args.steps, dev)}))
 
 
+def cnlse_setup(dev):
+    """The coupled 1024^2 configuration: CNLSE, both components, Gaussian nonlocal
+    kernel (sigma 100 um on a 67^2 support), L = 20 mm at dz = 5e-5 (400 steps)."""
+    import torch
+
+    import nlse_gb300 as ng
+
+    NC, LC = 1024, 20e-3
+    s3 = ng.CNLSE(ALPHA, 0.5, 4 * WAIST, N2, -0.8e-9, None, LC, NX=NC, NY=NC, Isat=ISAT,
+                  nl_length=100e-6)
+    s3.delta_z, s3.power2, s3.n22 = 5e-5, 0.05, N2
+    dxc = 4 * WAIST / NC
+    rr = np.arange(-33, 34) * dxc
+    kern = np.exp(-(rr[:, None] ** 2 + rr[None, :] ** 2) / (2 * (100e-6) ** 2))
+    s3.nl_profile = kern / kern.sum()
+    E3 = np.array([np.exp(-(s3.XX**2 + s3.YY**2) / w**2) for w in (1.5e-3, 0.5e-3)])
+    return s3, torch.from_numpy(E3.astype(np.complex64)).to(dev), LC
+
+
+def cnlse_only(args):
+    """Three out_field calls of the CNLSE nonlocal configuration (the last one timed)."""
+    import torch
+
+    from nlse_gb300 import _build
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    s3, E3, _ = cnlse_setup(dev)
+    z = (args.cnlse_only - 0.5) * 5e-5
+    for _ in range(2):
+        s3.out_field(E3, z, verbose=False)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    s3.out_field(E3, z, verbose=False)
+    b.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    print(json.dumps({"cnlse_1024_nonlocal_only": {"steps": args.cnlse_only,
+                                                   "steps_per_s": round(args.cnlse_only / t, 1)}}))
+
+
 def network_only(args):
     """Inference throughput of an initialised surrogate network on random inputs."""
     import torch
@@ -669,6 +705,8 @@ def main():
     args = parse()
     if args.network_only:
         network_only(args)
+    elif args.cnlse_only:
+        cnlse_only(args)
     elif args.mixed_only:
         mixed_only(args)
     elif args.impl == "reference":
