@@ -95,6 +95,15 @@ def _pipeline_streams(dev: torch.device) -> tuple:
     return _PIPE_STREAMS[key]
 
 
+def pipeline_split(nf: int, nbytes: int, nsteps: int, max_steps: int, min_bytes: int):
+    """Field bounds of the host pipeline's chunks for a batch of nf fields of
+    nbytes in all, propagated over nsteps steps, or None (not pipelined): the
+    first and the last field alone, the others together."""
+    if nf < 2 or nbytes < min_bytes or nsteps > max_steps:
+        return None
+    return [0, 1, nf] if nf < 4 else [0, 1, nf - 1, nf]
+
+
 class NLSE:
     """A class to solve NLSE"""
 
@@ -587,9 +596,8 @@ class NLSE:
             return None
         lead = self._lead_shape(tuple(E_in.shape))
         nf = int(np.prod(lead)) if lead else 1
-        if nf < 2 or E_in.numel() * E_in.element_size() < self.PIPELINE_MIN_BYTES:
-            return None
-        return [0, 1, nf] if nf < 4 else [0, 1, nf - 1, nf]
+        return pipeline_split(nf, E_in.numel() * E_in.element_size(), nsteps,
+                              self.PIPELINE_MAX_STEPS, self.PIPELINE_MIN_BYTES)
 
     def _out_field_pipelined(self, E_in: torch.Tensor, z: float, precision: str, verbose: bool,
                              normalize: bool, bounds: list) -> torch.Tensor:

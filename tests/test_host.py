@@ -304,3 +304,18 @@ def test_surrogate_constants_match_the_header():
     assert (fno.PART_LAYER, fno.PART_PROJ, fno.PART_LIFT) == (
         d["PART_LAYER"], d["PART_PROJ"], d["PART_LIFT"])
     assert d["PART_LAYER"] == d["C"] * d["C"] + d["C"] and d["PART_PROJ"] == 2 * d["C"] + 2
+
+
+def test_pipeline_split_policy():
+    """Host pipeline chunks: first and last field alone, only for short loops
+    of large enough batches."""
+    from nlse_gb300.nlse import NLSE, pipeline_split
+
+    mx, mn = NLSE.PIPELINE_MAX_STEPS, NLSE.PIPELINE_MIN_BYTES
+    assert pipeline_split(8, 1 << 28, 20, mx, mn) == [0, 1, 7, 8]
+    assert pipeline_split(4, 1 << 28, mx, mx, mn) == [0, 1, 3, 4]
+    assert pipeline_split(3, 1 << 28, 20, mx, mn) == [0, 1, 3]
+    assert pipeline_split(2, 1 << 28, 20, mx, mn) == [0, 1, 2]
+    assert pipeline_split(1, 1 << 28, 20, mx, mn) is None
+    assert pipeline_split(8, mn - 1, 20, mx, mn) is None
+    assert pipeline_split(8, 1 << 28, mx + 1, mx, mn) is None
