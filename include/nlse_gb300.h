@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NLSE_ABI_VERSION 1
+#define NLSE_ABI_VERSION 2
 
 typedef enum { NLSE_C64 = 0, NLSE_C128 = 1 } nlse_dtype;
 

@@ -188,7 +188,7 @@ def load(path: str | Path | None = None) -> ct.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.nlse_abi_version() != 1:
+        if lib.nlse_abi_version() != 2:
             raise RuntimeError("libnlse_sm103 ABI version mismatch")
         _lib = lib
         return lib

@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_error_reporting(lib):
-    assert lib.nlse_abi_version() == 1
+    assert lib.nlse_abi_version() == 2
     h = ct.c_void_p()
     d = _lib.Desc()
     d.ndim = 2
